@@ -1,0 +1,144 @@
+// co_internal.cuh -- shared declarations of the collops GB300 library.
+//
+// One context (co_ctx) per (mesh, device): it owns the mesh tables in HBM, the
+// marker-sized device buffers (reallocated only when N grows), one CUDA stream,
+// and the device-side solver state. All kernels are hand-written for sm_103a;
+// the host side only sequences launches and copies.
+//
+// Device data layout (all FP64 unless noted):
+//   markers  SoA, Julia column-major N x 2: x[0..N) = v1, x[N..2N) = v2
+//   sorted   in-domain markers in (cell, index) order: sx1, sx2, sw, perm, scell
+//   coeffs   n_dofs vectors indexed i1 + i2*nd1 (first dimension fastest)
+//   packed   pair-sum operands in sorted order: px = {v1,v2} (double2),
+//            pg = {G1,G2} (double2), pw (double); FP32 copies for the mixed form
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/collops.h"
+
+#define CO_CHUNK 1024        // markers per sort chunk (one block of 1024 threads)
+#define CO_RED_THREADS 256   // threads of the reduction-producing kernels
+#define CO_MAX_M 8           // Anderson depth limit of the device solver
+#define CO_FS_FLOOR 1e-30    // functions.jl:23
+#define CO_G_MAX 100.0       // functions.jl:31
+
+// Device-side solver state, mirrored from step_anderson!'s locals
+// (solver.jl:320-332) and read back by the host each iteration.
+struct co_solver_state {
+    int k;               // current iteration (1-based)
+    int history, slot;   // Anderson window (solver.jl:320-321)
+    int n_restart;
+    int done;            // 0 running, 1 converged, 2 stagnated, 3 max_iter
+    int path;            // 0 damped Picard, 1 Anderson, for the current k
+    int improved;        // nrm_r < nrm_best at the current k
+    int error;           // device-detected error (non-finite residual, timeout)
+    double nrm_r0, nrm_r, nrm_v, nrm_best, nrm_best_window, damp, res_out;
+    double ATA[CO_MAX_M * CO_MAX_M];
+    double gamma[CO_MAX_M];
+    double lambda;       // Gonzalez correction of the current map
+    double S1;           // entropy of v_in's projection
+    double lb[8];        // LB: n, U1, U2, Q, Sg1, Sg2, P  (+ spare)
+    double ab[3];        // LB multipliers A1, A2, B
+};
+
+struct co_bufs {
+    int cap;             // marker capacity
+    int nchunk_cap;
+    // per-marker (original order)
+    double *vmid, *dv, *G, *dS, *Gv, *r, *rp, *Gp, *vbest, *v1, *v0, *w, *vin, *dotv;
+    int *cell, *inv;
+    double *xi;          // 2N: xi1, xi2
+    // sorted in-domain markers
+    int *perm, *scell;
+    double *sw, *sphi;   // sphi: 6 per marker (phi1[3], phi2[3])
+    // packed pair operands
+    double2 *px, *pg;
+    double *pw;
+    float4 *pf_x;        // {x1h, x2h, x1l, x2l}
+    float4 *pf_g;        // {g1h, g2h, g1l, g2l}
+    float *pf_w;
+    double *pdot;        // packed vdot (2 x cap)
+    double *pA;          // packed metric A (3 x cap)
+    double *part;        // slice partials of the pair kernels
+    size_t part_cap;
+    // sort scratch
+    int *hist, *hoff, *count, *cstart;
+    // reductions
+    double *red;         // block partials (sized for the largest grid)
+    int red_cap;
+    // Anderson window
+    double *dF, *dG;     // 2N x m each
+    int m_cap;
+};
+
+struct co_ctx {
+    int device;
+    cudaStream_t stream;
+    unsigned flags;
+    int n1, n2, nd1, nd2, n_dofs, n_el, nq;
+    double lo1, hi1, lo2, hi2;
+    // mesh tables
+    double *bp1, *bp2;       // breakpoints
+    double *C1, *C2;         // extraction [n][9]
+    double *Tq1, *Tq2;       // basis at quad nodes: [n][3][nq]
+    double *qw;              // quad weights [nq]
+    double *Minv1, *Minv2;   // inverse 1D mass matrices (nd x nd, symmetric)
+    // coefficient-sized buffers
+    double *bS;              // cell sums [n_el][9]
+    double *b, *y, *f, *fin, *rr, *L;  // n_dofs each
+    double *E;               // element-local r contributions [n_el][9]
+    double *Ep;              // element entropy partials [n_el]
+    co_bufs mb;
+    co_solver_state *st;     // device state
+    co_solver_state *st_host;  // pinned mirror
+    double *hstage;          // pinned host staging (grows)
+    size_t hstage_cap;
+    int pair_split_fp64, pair_split_fp32;  // autotuned split factors (0 = auto)
+    int nsm;
+    // launch counter (kernels of this library launched through the context)
+    unsigned long long launches;
+};
+
+// ------------------------------------------------------------- helpers
+#define CO_CK(call)                                                   \
+    do {                                                              \
+        cudaError_t e_ = (call);                                      \
+        if (e_ != cudaSuccess) return CO_ERR_CUDA;                    \
+    } while (0)
+
+static inline int co_cdiv(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// ------------------------------------------------------------- spline stage
+// (co_spline.cu)
+int co_ensure_capacity(co_ctx *c, int N, int m);
+int co_sort_markers(co_ctx *c, const double *x, int N);       // locate + stable cell sort
+int co_project_sorted(co_ctx *c, double *f_out);               // scatter + dof gather + mass solve
+int co_mass_solve_dev(co_ctx *c, const double *rhs, double *out);
+int co_compute_r_dev(co_ctx *c, const double *f, double *r);
+int co_entropy_parts_dev(co_ctx *c, const double *f);          // fills c->Ep
+int co_entropy_finalize_dev(co_ctx *c, double *S_dev);         // sums Ep -> *S_dev
+int co_grad_L_dev(co_ctx *c, const double *x, int N, const double *L, double *G,
+                  const double *w, double *dS, const double *dv, double *red);
+int co_loggrad_dev(co_ctx *c, const double *x, int N, const double *f, double *g,
+                   const double *w, const double *dv, double *red);
+int co_mid_dv(co_ctx *c, const double *vin, const double *v0, int N);
+
+// ------------------------------------------------------------- pair stage
+// (co_pair.cu)
+int co_pair_fp64(co_ctx *c, int M, int with_metric);   // packed -> pdot (and pA)
+int co_pair_fp32(co_ctx *c, int M);                    // packed FP32 -> pdot
+int co_pack_landau(co_ctx *c, int N, int Mub, int precision, int gonzalez);
+int co_pack_plain(co_ctx *c, int N, int Mub, int precision, const double *x, const double *G);
+int co_unpack_A(co_ctx *c, int N, double *A);
+int co_unpack_update(co_ctx *c, int N, double dt, double *Gv, const double *v0,
+                     const double *v1, double *r, double *red);
+
+// ------------------------------------------------------------- solver stage
+// (co_solver.cu)
+int co_picard_map_dev(co_ctx *c, const co_opts *o, int precision, double *Gv,
+                      const double *vin, const double *v0, const double *w, int N,
+                      double S0, double dt, int want_resid);
+int co_lb_fused(co_ctx *c, int N, double nu, double dt, double *Gv, const double *v0,
+                const double *vmid, const double *w, double *g, const double *dv,
+                int gonzalez, const double *v1, double *r);

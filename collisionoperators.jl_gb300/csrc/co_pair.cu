@@ -1,0 +1,494 @@
+// co_pair.cu -- the O(N^2) Landau pair sum (functions.jl:205-237) on sm_103a.
+//
+// N-body layout: the in-domain markers are compacted and cell-sorted by the
+// spline stage; the pack kernel lays their operands out contiguously (px, pg,
+// pw). A block owns a tile of targets gamma (one per thread) and streams the
+// sources alpha through shared memory in tiles; the alpha range can be split
+// into slices whose partial sums are added afterwards in slice order, so
+// results are bitwise reproducible for a given N.
+//
+// FP64 form (the reference's Float64 path): on GB300 FP64 issues at 1/64 of
+// the FP32 rate, so the per-pair FP64 instruction count is what sets the time.
+// The pair body is 20 FP64 instructions:
+//   d (2), |d|^2 (2), 1/|d| refinement (5), G difference (2), d.g (2),
+//   1/|d|^2 and (d.g)/|d|^2 (2), projection (2), w/|d| (1), accumulate (2).
+// 1/|d| starts from a single-precision seed built from the FP64 bit pattern
+// with integer operations (no FP64 conversion instructions) and MUFU.RSQ, then
+// one third-order Newton step y += y e (1/2 + 3/8 e), e = 1 - x y^2, which
+// takes the ~2^-20 seed error to below 2^-53 (the same idea as the
+// reference's f32 seed + two Newton steps, collision_gpu.jl:36-44, with one
+// higher-order step in place of two quadratic ones). The |d|^2 < 1e-24 guard
+// (functions.jl:224) is an integer compare on the bit pattern.
+//
+// Mixed form (BASELINE precision form): the pair arithmetic runs in FP32 on
+// FP64-centred differences -- each coordinate is split into an FP32 head and
+// tail (x = xh + xl), so d = (xh_g - xh_a) + (xl_g - xl_a) is accurate to an
+// FP32 rounding of d itself even for close pairs -- and the per-tile FP32
+// partial sums are accumulated in FP64.
+#include "co_internal.cuh"
+#include "co_reduce.cuh"
+
+#define PAIR_TPB 128
+
+// bit pattern of 1e-24 (functions.jl:224 guard)
+#define CO_R2_MIN_BITS 0x3B282DB34012B251LL
+
+__device__ __forceinline__ double rsqrt_seed64(double x) {
+    // FP32 value of x from its high word (x in [1e-30, 1e30], positive)
+    int hi = __double2hiint(x);
+    float xf = __int_as_float((hi - (896 << 20)) << 3);
+    float yf = rsqrtf(xf);
+    int fb = __float_as_int(yf);
+    return __hiloint2double((fb >> 3) + (896 << 20), fb << 29);
+}
+
+__device__ __forceinline__ void pair64(double xg1, double xg2, double Gg1, double Gg2,
+                                       double xa1, double xa2, double Ga1, double Ga2,
+                                       double wa, double &acc1, double &acc2) {
+    double d1 = xg1 - xa1;
+    double d2 = xg2 - xa2;
+    double r2 = d1 * d1;
+    r2 = fma(d2, d2, r2);
+    bool ok = __double_as_longlong(r2) >= CO_R2_MIN_BITS;
+    double xr = ok ? r2 : 1.0;
+    double y = rsqrt_seed64(xr);
+    double t = xr * y;
+    double e = fma(-t, y, 1.0);
+    double p = fma(0.375, e, 0.5);
+    double ye = y * e;
+    y = fma(ye, p, y);
+    double g1 = Ga1 - Gg1;
+    double g2 = Ga2 - Gg2;
+    double dg = d1 * g1;
+    dg = fma(d2, g2, dg);
+    double y2 = y * y;
+    double cc = dg * y2;
+    double t1 = fma(-d1, cc, g1);
+    double t2 = fma(-d2, cc, g2);
+    double s = wa * y;
+    s = ok ? s : 0.0;
+    acc1 = fma(s, t1, acc1);
+    acc2 = fma(s, t2, acc2);
+}
+
+// F and the metric A (functions.jl:249-290 / collision_gpu.jl:289-339)
+__device__ __forceinline__ void pair64_metric(double xg1, double xg2, double Gg1, double Gg2,
+                                              double xa1, double xa2, double Ga1, double Ga2,
+                                              double wa, double &acc1, double &acc2,
+                                              double &a11, double &a12, double &a22) {
+    double d1 = xg1 - xa1;
+    double d2 = xg2 - xa2;
+    double q11 = d1 * d1, q22 = d2 * d2;
+    double r2 = q11 + q22;
+    bool ok = __double_as_longlong(r2) >= CO_R2_MIN_BITS;
+    double xr = ok ? r2 : 1.0;
+    double y = rsqrt_seed64(xr);
+    double t = xr * y;
+    double e = fma(-t, y, 1.0);
+    double p = fma(0.375, e, 0.5);
+    double ye = y * e;
+    y = fma(ye, p, y);
+    double g1 = Ga1 - Gg1;
+    double g2 = Ga2 - Gg2;
+    double dg = d1 * g1;
+    dg = fma(d2, g2, dg);
+    double y2 = y * y;
+    double cc = dg * y2;
+    double t1 = fma(-d1, cc, g1);
+    double t2 = fma(-d2, cc, g2);
+    double s = wa * y;
+    s = ok ? s : 0.0;
+    acc1 = fma(s, t1, acc1);
+    acc2 = fma(s, t2, acc2);
+    a11 = fma(s, fma(-q11, y2, 1.0), a11);
+    a12 = fma(-s, (d1 * d2) * y2, a12);
+    a22 = fma(s, fma(-q22, y2, 1.0), a22);
+}
+
+// out layout: partial[slice][comp][M] with stride ld
+template <bool METRIC>
+__global__ void __launch_bounds__(PAIR_TPB)
+k_pair64(const double2 *__restrict__ px, const double2 *__restrict__ pg,
+         const double *__restrict__ pw, const int *__restrict__ Mp, int slice_len,
+         double *__restrict__ out, size_t ld) {
+    __shared__ double2 sx[PAIR_TPB];
+    __shared__ double2 sg[PAIR_TPB];
+    __shared__ double sw[PAIR_TPB];
+    const int M = *Mp;
+    const int g0 = blockIdx.x * PAIR_TPB;
+    if (g0 >= M) return;
+    const int g = g0 + threadIdx.x;
+    const int sl = blockIdx.y;
+    const int a0 = sl * slice_len;
+    const int a1 = min(M, a0 + slice_len);
+    double2 xg = make_double2(0.0, 0.0), Gg = make_double2(0.0, 0.0);
+    if (g < M) {
+        xg = px[g];
+        Gg = pg[g];
+    }
+    double acc1 = 0.0, acc2 = 0.0, a11 = 0.0, a12 = 0.0, a22 = 0.0;
+    for (int base = a0; base < a1; base += PAIR_TPB) {
+        int a = base + threadIdx.x;
+        if (a < a1) {
+            sx[threadIdx.x] = px[a];
+            sg[threadIdx.x] = pg[a];
+            sw[threadIdx.x] = pw[a];
+        } else {  // inert padding: far away, zero weight
+            sx[threadIdx.x] = make_double2(1e3, 1e3);
+            sg[threadIdx.x] = make_double2(0.0, 0.0);
+            sw[threadIdx.x] = 0.0;
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int k = 0; k < PAIR_TPB; k++) {
+            double2 xa = sx[k], Ga = sg[k];
+            if (METRIC)
+                pair64_metric(xg.x, xg.y, Gg.x, Gg.y, xa.x, xa.y, Ga.x, Ga.y, sw[k], acc1, acc2,
+                              a11, a12, a22);
+            else
+                pair64(xg.x, xg.y, Gg.x, Gg.y, xa.x, xa.y, Ga.x, Ga.y, sw[k], acc1, acc2);
+        }
+        __syncthreads();
+    }
+    if (g < M) {
+        const int nc = METRIC ? 5 : 2;
+        double *o = out + (size_t)sl * nc * ld;
+        o[g] = acc1;
+        o[ld + g] = acc2;
+        if (METRIC) {
+            o[2 * ld + g] = a11;
+            o[3 * ld + g] = a12;
+            o[4 * ld + g] = a22;
+        }
+    }
+}
+
+// FP32 pair body on head/tail-split operands
+__device__ __forceinline__ void pair32(const float4 &xg, const float4 &Gg, const float4 &xa,
+                                       const float4 &Ga, float wa, float &acc1, float &acc2) {
+    float d1 = (xg.x - xa.x) + (xg.z - xa.z);
+    float d2 = (xg.y - xa.y) + (xg.w - xa.w);
+    float g1 = (Ga.x - Gg.x) + (Ga.z - Gg.z);
+    float g2 = (Ga.y - Gg.y) + (Ga.w - Gg.w);
+    float r2 = d1 * d1;
+    r2 = fmaf(d2, d2, r2);
+    float y = rsqrtf(r2);
+    y = r2 >= 1e-24f ? y : 0.0f;
+    float dg = d1 * g1;
+    dg = fmaf(d2, g2, dg);
+    float y2 = y * y;
+    float cc = dg * y2;
+    float t1 = fmaf(-d1, cc, g1);
+    float t2 = fmaf(-d2, cc, g2);
+    float s = wa * y;
+    acc1 = fmaf(s, t1, acc1);
+    acc2 = fmaf(s, t2, acc2);
+}
+
+#define PAIR32_TILE 256
+__global__ void __launch_bounds__(PAIR_TPB)
+k_pair32(const float4 *__restrict__ pfx, const float4 *__restrict__ pfg,
+         const float *__restrict__ pfw, const int *__restrict__ Mp, int slice_len,
+         double *__restrict__ out, size_t ld) {
+    __shared__ float4 sx[PAIR32_TILE];
+    __shared__ float4 sg[PAIR32_TILE];
+    __shared__ float sw[PAIR32_TILE];
+    const int M = *Mp;
+    const int g0 = blockIdx.x * PAIR_TPB;
+    if (g0 >= M) return;
+    const int g = g0 + threadIdx.x;
+    const int sl = blockIdx.y;
+    const int a0 = sl * slice_len;
+    const int a1 = min(M, a0 + slice_len);
+    float4 xg = make_float4(0.f, 0.f, 0.f, 0.f), Gg = xg;
+    if (g < M) {
+        xg = pfx[g];
+        Gg = pfg[g];
+    }
+    double acc1 = 0.0, acc2 = 0.0;
+    for (int base = a0; base < a1; base += PAIR32_TILE) {
+        for (int k = threadIdx.x; k < PAIR32_TILE; k += PAIR_TPB) {
+            int a = base + k;
+            if (a < a1) {
+                sx[k] = pfx[a];
+                sg[k] = pfg[a];
+                sw[k] = pfw[a];
+            } else {
+                sx[k] = make_float4(1e3f, 1e3f, 0.f, 0.f);
+                sg[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+                sw[k] = 0.f;
+            }
+        }
+        __syncthreads();
+        float t1 = 0.f, t2 = 0.f;
+#pragma unroll 8
+        for (int k = 0; k < PAIR32_TILE; k++) pair32(xg, Gg, sx[k], sg[k], sw[k], t1, t2);
+        acc1 += (double)t1;
+        acc2 += (double)t2;
+        __syncthreads();
+    }
+    if (g < M) {
+        double *o = out + (size_t)sl * 2 * ld;
+        o[g] = acc1;
+        o[ld + g] = acc2;
+    }
+}
+
+// sum the slice partials of components [c0, c0+nc) in slice order into
+// dst (nc x ld); the partials hold ncomp components per slice
+__global__ void k_slice_reduce(const double *__restrict__ part, int split, int ncomp, int c0,
+                               int nc, size_t ld, const int *__restrict__ Mp,
+                               double *__restrict__ dst) {
+    int M = *Mp;
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= M) return;
+    for (int c = 0; c < nc; c++) {
+        double s = 0.0;
+        for (int sl = 0; sl < split; sl++) s += part[((size_t)sl * ncomp + c0 + c) * ld + g];
+        dst[(size_t)c * ld + g] = s;
+    }
+}
+
+// Landau pack: lambda from the device state, G_eff = -(dS + lambda dv)/w
+// (solver.jl:107-111), operands in sorted order.
+__global__ void k_pack_landau(const int *__restrict__ perm, const int *__restrict__ Mp, int N,
+                              const double *__restrict__ vmid, const double *__restrict__ dS,
+                              const double *__restrict__ dv, const double *__restrict__ w,
+                              const co_solver_state *__restrict__ st, int use_lambda,
+                              int precision, double2 *__restrict__ px, double2 *__restrict__ pg,
+                              double *__restrict__ pw, float4 *__restrict__ pfx,
+                              float4 *__restrict__ pfg, float *__restrict__ pfw) {
+    int M = *Mp;
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= M) return;
+    int a = perm[p];
+    double lam = use_lambda ? st->lambda : 0.0;
+    double iw = 1.0 / w[a];
+    double x1 = vmid[a], x2 = vmid[N + a];
+    double G1 = -(dS[a] + lam * dv[a]) * iw;
+    double G2 = -(dS[N + a] + lam * dv[N + a]) * iw;
+    if (precision == CO_PREC_MIXED) {
+        float x1h = (float)x1, x2h = (float)x2, G1h = (float)G1, G2h = (float)G2;
+        pfx[p] = make_float4(x1h, x2h, (float)(x1 - (double)x1h), (float)(x2 - (double)x2h));
+        pfg[p] = make_float4(G1h, G2h, (float)(G1 - (double)G1h), (float)(G2 - (double)G2h));
+        pfw[p] = (float)w[a];
+    } else {
+        px[p] = make_double2(x1, x2);
+        pg[p] = make_double2(G1, G2);
+        pw[p] = w[a];
+    }
+}
+
+// Hook pack: operands straight from (v, G, w) (COLLISION_FN semantics).
+__global__ void k_pack_plain(const int *__restrict__ perm, const int *__restrict__ Mp, int N,
+                             const double *__restrict__ v, const double *__restrict__ G,
+                             const double *__restrict__ w, int precision,
+                             double2 *__restrict__ px, double2 *__restrict__ pg,
+                             double *__restrict__ pw, float4 *__restrict__ pfx,
+                             float4 *__restrict__ pfg, float *__restrict__ pfw) {
+    int M = *Mp;
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= M) return;
+    int a = perm[p];
+    double x1 = v[a], x2 = v[N + a], G1 = G[a], G2 = G[N + a];
+    if (precision == CO_PREC_MIXED) {
+        float x1h = (float)x1, x2h = (float)x2, G1h = (float)G1, G2h = (float)G2;
+        pfx[p] = make_float4(x1h, x2h, (float)(x1 - (double)x1h), (float)(x2 - (double)x2h));
+        pfg[p] = make_float4(G1h, G2h, (float)(G1 - (double)G1h), (float)(G2 - (double)G2h));
+        pfw[p] = (float)w[a];
+    } else {
+        px[p] = make_double2(x1, x2);
+        pg[p] = make_double2(G1, G2);
+        pw[p] = w[a];
+    }
+}
+
+// Gv = v0 + dt * vdot (solver.jl:225), vdot unpacked from sorted order (0 for
+// out-of-domain markers); optionally r = Gv - v1 and block partials of |r|^2,
+// |v1|^2 for step_anderson! (solver.jl:339-349).
+__global__ void __launch_bounds__(CO_RED_THREADS)
+k_unpack_update(const int *__restrict__ inv, int N, const double *__restrict__ pdot, size_t ld,
+                double dt, const double *__restrict__ v0, double *__restrict__ Gv,
+                double *__restrict__ dotv, const double *__restrict__ v1, double *__restrict__ r,
+                double *__restrict__ red) {
+    __shared__ double sh[32];
+    double sr = 0.0, sv = 0.0;
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < N; a += gridDim.x * blockDim.x) {
+        int p = inv[a];
+        double q1 = 0.0, q2 = 0.0;
+        if (p >= 0) {
+            q1 = pdot[p];
+            q2 = pdot[ld + p];
+        }
+        if (dotv) {
+            dotv[a] = q1;
+            dotv[N + a] = q2;
+        }
+        if (Gv) {
+            double g1 = v0[a] + dt * q1, g2 = v0[N + a] + dt * q2;
+            Gv[a] = g1;
+            Gv[N + a] = g2;
+            if (r) {
+                double x1 = v1[a], x2 = v1[N + a];
+                double r1 = g1 - x1, r2 = g2 - x2;
+                r[a] = r1;
+                r[N + a] = r2;
+                sr += r1 * r1 + r2 * r2;
+                sv += x1 * x1 + x2 * x2;
+            }
+        }
+    }
+    if (red) {
+        double a = co_block_sum(sr, sh);
+        double b = co_block_sum(sv, sh);
+        if (threadIdx.x == 0) {
+            red[blockIdx.x * 2 + 0] = a;
+            red[blockIdx.x * 2 + 1] = b;
+        }
+    }
+}
+
+// unpack A (3 comps) for COLLMETRIC_FN
+__global__ void k_unpack_A(const int *__restrict__ inv, int N, const double *__restrict__ pA,
+                           size_t ld, double *__restrict__ A) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= N) return;
+    int p = inv[a];
+    for (int c = 0; c < 3; c++) A[(size_t)c * N + a] = p >= 0 ? pA[(size_t)c * ld + p] : 0.0;
+}
+
+// ------------------------------------------------------------------ host
+
+static int choose_split(co_ctx *c, int M, int tpb, int force) {
+    if (force > 0) return force;
+    int tiles = co_cdiv(M, tpb);
+    if (tiles < 1) tiles = 1;
+    int want = co_cdiv(4LL * c->nsm, tiles);
+    int max_split = co_cdiv(M, 256);
+    if (max_split < 1) max_split = 1;
+    if (want > max_split) want = max_split;
+    if (want < 1) want = 1;
+    return want;
+}
+
+static int ensure_part(co_ctx *c, size_t n) {
+    if (n <= c->mb.part_cap) return CO_OK;
+    if (c->mb.part) cudaFree(c->mb.part);
+    c->mb.part = nullptr;
+    if (cudaMalloc(&c->mb.part, n * sizeof(double)) != cudaSuccess) return CO_ERR_NOMEM;
+    c->mb.part_cap = n;
+    return CO_OK;
+}
+
+// M is an upper bound (N); the true count sits at cstart[n_el] on the device.
+int co_pair_fp64(co_ctx *c, int Mub, int with_metric) {
+    if (Mub <= 0) return CO_OK;
+    const int *Mp = c->mb.cstart + c->n_el;
+    size_t ld = (size_t)c->mb.cap;
+    int split = choose_split(c, Mub, PAIR_TPB, c->pair_split_fp64);
+    int slice = co_cdiv(Mub, split);
+    slice = co_cdiv(slice, PAIR_TPB) * PAIR_TPB;
+    split = co_cdiv(Mub, slice);
+    int nc = with_metric ? 5 : 2;
+    dim3 grid(co_cdiv(Mub, PAIR_TPB), split);
+    double *dst = c->mb.pdot;
+    if (split > 1 || with_metric) {
+        int rc = ensure_part(c, (size_t)split * nc * ld);
+        if (rc) return rc;
+        dst = c->mb.part;
+    }
+    if (with_metric)
+        k_pair64<true><<<grid, PAIR_TPB, 0, c->stream>>>(c->mb.px, c->mb.pg, c->mb.pw, Mp, slice,
+                                                         dst, ld);
+    else
+        k_pair64<false><<<grid, PAIR_TPB, 0, c->stream>>>(c->mb.px, c->mb.pg, c->mb.pw, Mp, slice,
+                                                          dst, ld);
+    c->launches++;
+    if (with_metric) {
+        // components 0,1 -> pdot ; 2,3,4 -> pA
+        k_slice_reduce<<<co_cdiv(Mub, 256), 256, 0, c->stream>>>(dst, split, 5, 0, 2, ld, Mp,
+                                                                c->mb.pdot);
+        k_slice_reduce<<<co_cdiv(Mub, 256), 256, 0, c->stream>>>(dst, split, 5, 2, 3, ld, Mp,
+                                                                c->mb.pA);
+        c->launches += 2;
+    } else if (split > 1) {
+        k_slice_reduce<<<co_cdiv(Mub, 256), 256, 0, c->stream>>>(dst, split, 2, 0, 2, ld, Mp,
+                                                                c->mb.pdot);
+        c->launches++;
+    }
+    CO_CK(cudaGetLastError());
+    return CO_OK;
+}
+
+int co_pair_fp32(co_ctx *c, int Mub) {
+    if (Mub <= 0) return CO_OK;
+    const int *Mp = c->mb.cstart + c->n_el;
+    size_t ld = (size_t)c->mb.cap;
+    int split = choose_split(c, Mub, PAIR_TPB, c->pair_split_fp32);
+    int slice = co_cdiv(Mub, split);
+    slice = co_cdiv(slice, PAIR32_TILE) * PAIR32_TILE;
+    split = co_cdiv(Mub, slice);
+    dim3 grid(co_cdiv(Mub, PAIR_TPB), split);
+    double *dst = c->mb.pdot;
+    if (split > 1) {
+        int rc = ensure_part(c, (size_t)split * 2 * ld);
+        if (rc) return rc;
+        dst = c->mb.part;
+    }
+    k_pair32<<<grid, PAIR_TPB, 0, c->stream>>>(c->mb.pf_x, c->mb.pf_g, c->mb.pf_w, Mp, slice, dst,
+                                               ld);
+    c->launches++;
+    if (split > 1) {
+        k_slice_reduce<<<co_cdiv(Mub, 256), 256, 0, c->stream>>>(dst, split, 2, 0, 2, ld, Mp,
+                                                                c->mb.pdot);
+        c->launches++;
+    }
+    CO_CK(cudaGetLastError());
+    return CO_OK;
+}
+
+int co_pack_plain(co_ctx *c, int N, int Mub, int precision, const double *x, const double *G) {
+    if (Mub <= 0) return CO_OK;
+    const int *Mp = c->mb.cstart + c->n_el;
+    co_bufs &b = c->mb;
+    k_pack_plain<<<co_cdiv(Mub, 256), 256, 0, c->stream>>>(b.perm, Mp, N, x, G, b.w, precision,
+                                                           b.px, b.pg, b.pw, b.pf_x, b.pf_g,
+                                                           b.pf_w);
+    c->launches++;
+    CO_CK(cudaGetLastError());
+    return CO_OK;
+}
+
+int co_pack_landau(co_ctx *c, int N, int Mub, int precision, int gonzalez) {
+    if (Mub <= 0) return CO_OK;
+    const int *Mp = c->mb.cstart + c->n_el;
+    co_bufs &b = c->mb;
+    k_pack_landau<<<co_cdiv(Mub, 256), 256, 0, c->stream>>>(
+        b.perm, Mp, N, b.vmid, b.dS, b.dv, b.w, c->st, gonzalez, precision, b.px, b.pg, b.pw,
+        b.pf_x, b.pf_g, b.pf_w);
+    c->launches++;
+    CO_CK(cudaGetLastError());
+    return CO_OK;
+}
+
+int co_unpack_update(co_ctx *c, int N, double dt, double *Gv, const double *v0,
+                     const double *v1, double *r, double *red) {
+    if (N == 0) return CO_OK;
+    int g = co_cdiv(N, CO_RED_THREADS);
+    if (g > c->mb.red_cap) g = c->mb.red_cap;
+    k_unpack_update<<<g, CO_RED_THREADS, 0, c->stream>>>(c->mb.inv, N, c->mb.pdot,
+                                                         (size_t)c->mb.cap, dt, v0, Gv,
+                                                         c->mb.dotv, v1, r, red);
+    c->launches++;
+    CO_CK(cudaGetLastError());
+    return CO_OK;
+}
+
+int co_unpack_A(co_ctx *c, int N, double *A) {
+    if (N == 0) return CO_OK;
+    k_unpack_A<<<co_cdiv(N, 256), 256, 0, c->stream>>>(c->mb.inv, N, c->mb.pA, (size_t)c->mb.cap,
+                                                       A);
+    c->launches++;
+    CO_CK(cudaGetLastError());
+    return CO_OK;
+}

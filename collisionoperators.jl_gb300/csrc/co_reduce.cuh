@@ -1,0 +1,33 @@
+// co_reduce.cuh -- fixed-order block reductions (deterministic run to run).
+#pragma once
+#include <cuda_runtime.h>
+
+// Sum of one double over a block of blockDim.x (multiple of 32, <= 1024)
+// threads; every thread gets the result. Fixed shuffle tree, then warp
+// partials summed in warp order by warp 0.
+__device__ __forceinline__ double co_block_sum(double v, double *sh /* >= 32 */) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    int nw = blockDim.x >> 5;
+    if (warp == 0) {
+        double s = lane < nw ? sh[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) sh[0] = s;
+    }
+    __syncthreads();
+    double r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+// Sum of red[0..n) * (stride) component `comp` by one block, fixed order:
+// thread t sums entries t, t+B, ... in order, then co_block_sum.
+__device__ __forceinline__ double co_sum_partials(const double *red, int n, int ncomp,
+                                                   int comp, double *sh) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s += red[(size_t)i * ncomp + comp];
+    return co_block_sum(s, sh);
+}

@@ -1,0 +1,650 @@
+// co_solver.cu -- Picard map orchestration, Gonzalez correction, the fused LB
+// drift, and step_anderson! entirely on the device.
+//
+// Picard map (solver.jl:176-227), Landau:
+//   [Gonzalez] sort(v_in) -> project -> f_in -> S1 (element quadrature)
+//   v_mid, dv -> sort(v_mid) -> project -> f -> r -> L = M^{-1} r
+//   -> grad L at v_mid (+ dS = -w G, + dv.dS and |dv|^2 block partials)
+//   -> lambda (one block, fixed order) -> pack G_eff -> pair sum -> unpack,
+//   Gv = v0 + dt vdot (+ Anderson residual partials)
+// LB: the same projection; the clamped log-gradient gather; then one
+//   cooperative kernel applies lambda, forms the seven moments, solves the
+//   3x3 system redundantly in every block and writes the drift and Gv.
+//
+// The Anderson control (solver.jl:334-417) runs in one-block kernels that own
+// the device state; the host only launches the fixed kernel sequence of an
+// iteration and reads the `done` word.
+#include <math.h>
+
+#include "co_internal.cuh"
+#include "co_reduce.cuh"
+
+#define CO_RED_COMPS 16
+#define CO_BARRIER_SPINS (1 << 22)
+
+// ---------------------------------------------------------------- lambda
+
+__global__ void __launch_bounds__(256)
+k_lambda(const double *__restrict__ red, int nred, co_solver_state *st, double S0,
+         int gonzalez) {
+    __shared__ double sh[32];
+    double dot = co_sum_partials(red, nred, 2, 0, sh);
+    double n2 = co_sum_partials(red, nred, 2, 1, sh);
+    if (threadIdx.x == 0) {
+        double lam = 0.0;
+        if (gonzalez) lam = n2 > 1e-30 ? (st->S1 - S0 - dot) / n2 : 0.0;
+        st->lambda = lam;
+    }
+}
+
+// ---------------------------------------------------------------- LB fused
+
+// Grid barrier for a cooperative launch (all blocks co-resident). The wait is
+// bounded: after CO_BARRIER_SPINS polls the block records a timeout in *err
+// and continues, so the kernel always terminates.
+__device__ __forceinline__ void grid_barrier(unsigned *counter, unsigned nblocks, int *err) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        unsigned old = atomicAdd(counter, 1u);
+        unsigned target = (old / nblocks + 1u) * nblocks;
+        int spins = 0;
+        while (*((volatile unsigned *)counter) < target) {
+            if (++spins > CO_BARRIER_SPINS) {
+                atomicExch(err, 1);
+                break;
+            }
+            __nanosleep(64);
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+__device__ void lu3_solve(double *M, double *b) {
+    // LU with partial pivoting (Julia's `\` on the 3x3 system, functions.jl:103-105)
+    int piv[3];
+    for (int k = 0; k < 3; k++) {
+        int p = k;
+        double mx = fabs(M[k * 3 + k]);
+        for (int i = k + 1; i < 3; i++)
+            if (fabs(M[i * 3 + k]) > mx) { mx = fabs(M[i * 3 + k]); p = i; }
+        piv[k] = p;
+        if (p != k)
+            for (int j = 0; j < 3; j++) { double t = M[k * 3 + j]; M[k * 3 + j] = M[p * 3 + j]; M[p * 3 + j] = t; }
+        for (int i = k + 1; i < 3; i++) {
+            M[i * 3 + k] /= M[k * 3 + k];
+            for (int j = k + 1; j < 3; j++) M[i * 3 + j] -= M[i * 3 + k] * M[k * 3 + j];
+        }
+    }
+    for (int k = 0; k < 3; k++) if (piv[k] != k) { double t = b[k]; b[k] = b[piv[k]]; b[piv[k]] = t; }
+    for (int i = 0; i < 3; i++) for (int j = 0; j < i; j++) b[i] -= M[i * 3 + j] * b[j];
+    for (int i = 2; i >= 0; i--) {
+        for (int j = i + 1; j < 3; j++) b[i] -= M[i * 3 + j] * b[j];
+        b[i] /= M[i * 3 + i];
+    }
+}
+
+// LB drift with exact momentum/energy multipliers (functions.jl:68-116,
+// solver.jl:205-221), Gonzalez lambda applied first (solver.jl:204-209).
+__global__ void __launch_bounds__(CO_RED_THREADS)
+k_lb_fused(int N, const double *__restrict__ vmid, const double *__restrict__ w,
+           double *__restrict__ g, const double *__restrict__ dv, int use_lambda, double nu,
+           double dt, const double *__restrict__ v0, double *__restrict__ Gv,
+           const double *__restrict__ v1, double *__restrict__ r, double *__restrict__ red7,
+           double *__restrict__ red2, co_solver_state *st, unsigned *bar, int *err) {
+    __shared__ double sh[32];
+    __shared__ double sol[3];
+    const double lam = use_lambda ? st->lambda : 0.0;
+    double m[7] = {0, 0, 0, 0, 0, 0, 0};
+    const int stride = gridDim.x * blockDim.x;
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < N; a += stride) {
+        double wa = w[a], x = vmid[a], y = vmid[N + a];
+        double g1 = g[a], g2 = g[N + a];
+        if (use_lambda) {
+            double iw = 1.0 / wa;
+            g1 -= lam * dv[a] * iw;
+            g2 -= lam * dv[N + a] * iw;
+            g[a] = g1;
+            g[N + a] = g2;
+        }
+        m[0] += wa;
+        m[1] += wa * x;
+        m[2] += wa * y;
+        m[3] += wa * (x * x + y * y);
+        m[4] += wa * g1;
+        m[5] += wa * g2;
+        m[6] += wa * (x * g1 + y * g2);
+    }
+    for (int k = 0; k < 7; k++) {
+        double s = co_block_sum(m[k], sh);
+        if (threadIdx.x == 0) red7[blockIdx.x * 8 + k] = s;
+    }
+    grid_barrier(bar, gridDim.x, err);
+    // every block reduces the partials in the same fixed order
+    double tot[7];
+    for (int k = 0; k < 7; k++) tot[k] = co_sum_partials(red7, gridDim.x, 8, k, sh);
+    if (threadIdx.x == 0) {
+        double M[9] = {tot[0], 0.0, tot[1], 0.0, tot[0], tot[2], tot[1], tot[2], tot[3]};
+        double b[3] = {-tot[4], -tot[5], -tot[6]};
+        lu3_solve(M, b);
+        sol[0] = b[0]; sol[1] = b[1]; sol[2] = b[2];
+        if (blockIdx.x == 0) {
+            for (int k = 0; k < 7; k++) st->lb[k] = tot[k];
+            st->ab[0] = b[0]; st->ab[1] = b[1]; st->ab[2] = b[2];
+        }
+    }
+    __syncthreads();
+    const double A1 = sol[0], A2 = sol[1], B = sol[2];
+    double sr = 0.0, sv = 0.0;
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < N; a += stride) {
+        double x = vmid[a], y = vmid[N + a];
+        double q1 = -nu * (g[a] + A1 + B * x);
+        double q2 = -nu * (g[N + a] + A2 + B * y);
+        double o1 = v0[a] + dt * q1, o2 = v0[N + a] + dt * q2;
+        Gv[a] = o1;
+        Gv[N + a] = o2;
+        if (r) {
+            double x1 = v1[a], x2 = v1[N + a];
+            double r1 = o1 - x1, r2 = o2 - x2;
+            r[a] = r1;
+            r[N + a] = r2;
+            sr += r1 * r1 + r2 * r2;
+            sv += x1 * x1 + x2 * x2;
+        }
+    }
+    if (r) {
+        double s1 = co_block_sum(sr, sh);
+        double s2 = co_block_sum(sv, sh);
+        if (threadIdx.x == 0) {
+            red2[blockIdx.x * 2 + 0] = s1;
+            red2[blockIdx.x * 2 + 1] = s2;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- Anderson
+
+struct co_dev_opts {
+    int use_anderson, exit_picard_step, m, max_iter, stag_window, damp_decay_start;
+    double tol, abs_floor, stag_rel_tol, damp_decay_factor, restart_factor, damping, reg_factor;
+};
+
+__global__ void k_state_reset(co_solver_state *st) {
+    if (threadIdx.x == 0) {
+        st->k = 0;
+        st->history = 0;
+        st->slot = 0;
+        st->n_restart = 0;
+        st->done = 0;
+        st->path = 0;
+        st->improved = 0;
+        st->error = 0;
+        st->nrm_r0 = 0.0;
+        st->nrm_r = 0.0;
+        st->nrm_best = INFINITY;
+        st->nrm_best_window = INFINITY;
+        st->res_out = 0.0;
+    }
+}
+
+// residual norms and the exit / restart / damping decisions of iteration k
+// (solver.jl:339-391)
+__global__ void __launch_bounds__(256)
+k_ctrl1(const double *__restrict__ red, int nred, co_solver_state *st, co_dev_opts o) {
+    __shared__ double sh[32];
+    if (st->done) return;
+    double r2 = co_sum_partials(red, nred, 2, 0, sh);
+    double v2 = co_sum_partials(red, nred, 2, 1, sh);
+    if (threadIdx.x != 0) return;
+    int k = st->k + 1;
+    st->k = k;
+    double nrm_r = sqrt(r2), nrm_v = sqrt(v2);
+    st->nrm_r = nrm_r;
+    st->nrm_v = nrm_v;
+    if (!isfinite(nrm_r)) {
+        st->error = CO_ERR_NONFINITE;
+        st->done = 4;
+        st->res_out = nrm_r;
+        return;
+    }
+    if (k == 1) st->nrm_r0 = nrm_r;
+    st->improved = 0;
+    if (nrm_r < st->nrm_best) {
+        st->nrm_best = nrm_r;
+        st->improved = 1;
+    }
+    double eff_tol = fmax(o.tol * (nrm_v + 1e-30), o.abs_floor);
+    if (nrm_r < eff_tol) {
+        st->done = 1;
+        st->res_out = nrm_r;
+        return;
+    }
+    if (k > o.stag_window && k % o.stag_window == 0) {
+        double rel = (st->nrm_best_window - st->nrm_best) / (st->nrm_best_window + 1e-30);
+        if (rel < o.stag_rel_tol) {
+            st->done = 2;
+            st->res_out = st->nrm_best;
+            return;
+        }
+        st->nrm_best_window = st->nrm_best;
+    }
+    int just_restarted = 0;
+    double rf = o.restart_factor > 0 ? o.restart_factor : INFINITY;
+    if (k > 1 && nrm_r > rf * st->nrm_best) {
+        st->history = 0;
+        st->slot = 0;
+        st->n_restart += 1;
+        just_restarted = 1;
+    }
+    st->damp = k > o.damp_decay_start ? o.damping * o.damp_decay_factor : o.damping;
+    if (k == 1 || just_restarted || !o.use_anderson) {
+        st->path = 0;
+    } else {
+        st->path = 1;
+        st->slot = st->slot % o.m + 1;
+        st->history = st->history + 1 < o.m ? st->history + 1 : o.m;
+    }
+    if (k == o.max_iter) {
+        // the host stops after this iteration; k_finish returns v_best
+        st->res_out = st->nrm_best;
+    }
+}
+
+// damped Picard branch (solver.jl:384) + best-iterate tracking (:343-346)
+__global__ void k_plain_update(int n2, co_solver_state *st, int exit_picard,
+                               double *__restrict__ v1, const double *__restrict__ Gv,
+                               const double *__restrict__ r, double *__restrict__ rp,
+                               double *__restrict__ Gp, double *__restrict__ vbest) {
+    if (st->done) return;
+    int path = st->path, improved = st->improved;
+    double damp = st->damp;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
+        double x = v1[i], g = Gv[i];
+        if (improved) vbest[i] = exit_picard ? g : x;
+        if (path == 0) {
+            v1[i] = damp * g + (1 - damp) * x;
+            rp[i] = r[i];
+            Gp[i] = g;
+        }
+    }
+}
+
+// new window column (solver.jl:393-394) and its dot products with the window
+// and with r; block partials laid out [block][2*CO_MAX_M]
+__global__ void __launch_bounds__(CO_RED_THREADS)
+k_anderson_cols(int n2, co_solver_state *st, const double *__restrict__ r,
+                double *__restrict__ rp, const double *__restrict__ Gv, double *__restrict__ Gp,
+                double *__restrict__ dF, double *__restrict__ dG, size_t ldF,
+                double *__restrict__ red) {
+    __shared__ double sh[32];
+    if (st->done || st->path != 1) return;
+    const int slot = st->slot - 1, hist = st->history;
+    double pa[CO_MAX_M], pb[CO_MAX_M];
+    for (int j = 0; j < CO_MAX_M; j++) pa[j] = pb[j] = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
+        double ri = r[i], gi = Gv[i];
+        double F = ri - rp[i];
+        double Gd = gi - Gp[i];
+        dF[(size_t)slot * ldF + i] = F;
+        dG[(size_t)slot * ldF + i] = Gd;
+        rp[i] = ri;
+        Gp[i] = gi;
+        for (int j = 0; j < hist; j++) {
+            double fj = j == slot ? F : dF[(size_t)j * ldF + i];
+            pa[j] += F * fj;
+            pb[j] += fj * ri;
+        }
+    }
+    for (int j = 0; j < hist; j++) {
+        double a = co_block_sum(pa[j], sh);
+        double b = co_block_sum(pb[j], sh);
+        if (threadIdx.x == 0) {
+            red[(size_t)blockIdx.x * 2 * CO_MAX_M + j] = a;
+            red[(size_t)blockIdx.x * 2 * CO_MAX_M + CO_MAX_M + j] = b;
+        }
+    }
+}
+
+// normal equations with Tikhonov shift, gamma = ATA \ ATr (solver.jl:396-409)
+__global__ void __launch_bounds__(256)
+k_anderson_solve(const double *__restrict__ red, int nred, co_solver_state *st, co_dev_opts o) {
+    __shared__ double sh[32];
+    __shared__ double dots[2 * CO_MAX_M];
+    if (st->done || st->path != 1) return;
+    const int slot = st->slot - 1, h = st->history;
+    for (int j = 0; j < h; j++) {
+        double a = co_sum_partials(red, nred, 2 * CO_MAX_M, j, sh);
+        double b = co_sum_partials(red, nred, 2 * CO_MAX_M, CO_MAX_M + j, sh);
+        if (threadIdx.x == 0) {
+            dots[j] = a;
+            dots[CO_MAX_M + j] = b;
+        }
+    }
+    if (threadIdx.x != 0) return;
+    for (int j = 0; j < h; j++) {
+        st->ATA[slot * CO_MAX_M + j] = dots[j];
+        st->ATA[j * CO_MAX_M + slot] = dots[j];
+    }
+    double A[CO_MAX_M * CO_MAX_M], b[CO_MAX_M];
+    for (int i = 0; i < h; i++) {
+        for (int j = 0; j < h; j++) A[i * h + j] = st->ATA[i * CO_MAX_M + j];
+        b[i] = dots[CO_MAX_M + i];
+    }
+    double dm = 0.0;
+    for (int j = 0; j < h; j++) dm += A[j * h + j];
+    dm /= h;
+    double l2 = o.reg_factor * dm + 1e-30;
+    for (int j = 0; j < h; j++) A[j * h + j] += l2;
+    int piv[CO_MAX_M];
+    for (int k = 0; k < h; k++) {
+        int p = k;
+        double mx = fabs(A[k * h + k]);
+        for (int i = k + 1; i < h; i++)
+            if (fabs(A[i * h + k]) > mx) { mx = fabs(A[i * h + k]); p = i; }
+        piv[k] = p;
+        if (p != k)
+            for (int j = 0; j < h; j++) { double t = A[k * h + j]; A[k * h + j] = A[p * h + j]; A[p * h + j] = t; }
+        for (int i = k + 1; i < h; i++) {
+            A[i * h + k] /= A[k * h + k];
+            for (int j = k + 1; j < h; j++) A[i * h + j] -= A[i * h + k] * A[k * h + j];
+        }
+    }
+    for (int k = 0; k < h; k++) if (piv[k] != k) { double t = b[k]; b[k] = b[piv[k]]; b[piv[k]] = t; }
+    for (int i = 0; i < h; i++) for (int j = 0; j < i; j++) b[i] -= A[i * h + j] * b[j];
+    for (int i = h - 1; i >= 0; i--) {
+        for (int j = i + 1; j < h; j++) b[i] -= A[i * h + j] * b[j];
+        b[i] /= A[i * h + i];
+    }
+    for (int j = 0; j < h; j++) st->gamma[j] = b[j];
+}
+
+// v1 = damp (Gv - dG gamma) + (1 - damp) v_old (solver.jl:410-412)
+__global__ void k_anderson_update(int n2, co_solver_state *st, double *__restrict__ v1,
+                                  const double *__restrict__ Gv, const double *__restrict__ dG,
+                                  size_t ldF) {
+    if (st->done || st->path != 1) return;
+    const int h = st->history;
+    const double damp = st->damp;
+    double gam[CO_MAX_M];
+    for (int j = 0; j < h; j++) gam[j] = st->gamma[j];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
+        double s = Gv[i];
+        for (int j = 0; j < h; j++) s += -1.0 * dG[(size_t)j * ldF + i] * gam[j];
+        v1[i] = damp * s + (1 - damp) * v1[i];
+    }
+}
+
+// exit copies (solver.jl:351, :361, :420)
+__global__ void k_finish(int n2, co_solver_state *st, int exit_picard, double *__restrict__ v1,
+                         const double *__restrict__ Gv, const double *__restrict__ vbest) {
+    int done = st->done, improved = st->improved;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
+        if (done == 1) {
+            if (exit_picard) v1[i] = Gv[i];
+        } else if (done == 2) {
+            v1[i] = improved ? (exit_picard ? Gv[i] : v1[i]) : vbest[i];
+        } else if (done == 0 || done == 3) {
+            v1[i] = vbest[i];
+        }
+    }
+}
+
+__global__ void k_set_done(co_solver_state *st, int v) {
+    if (threadIdx.x == 0 && st->done == 0) st->done = v;
+}
+
+// ---------------------------------------------------------------- host
+
+static int ew_grid(co_ctx *c, long long n) {
+    int g = co_cdiv(n, 256);
+    int cap = 8 * c->nsm;
+    return g < 1 ? 1 : (g > cap ? cap : g);
+}
+
+static int red_blocks(co_ctx *c, int N) {
+    int g = co_cdiv(N, CO_RED_THREADS);
+    if (g > c->mb.red_cap) g = c->mb.red_cap;
+    return g < 1 ? 1 : g;
+}
+
+// Gonzalez entropy S1 of v_in's projection into st->S1
+static int entropy_into_state(co_ctx *c, const double *x, int N) {
+    int rc;
+    if ((rc = co_sort_markers(c, x, N))) return rc;
+    if ((rc = co_project_sorted(c, c->fin))) return rc;
+    if ((rc = co_entropy_parts_dev(c, c->fin))) return rc;
+    return co_entropy_finalize_dev(c, &c->st->S1);
+}
+
+int co_lb_fused(co_ctx *c, int N, double nu, double dt, double *Gv, const double *v0,
+                const double *vmid, const double *w, double *g, const double *dv,
+                int gonzalez, const double *v1, double *r) {
+    static int max_blocks_per_sm = -1;
+    if (max_blocks_per_sm < 0) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_blocks_per_sm, k_lb_fused,
+                                                          CO_RED_THREADS, 0) != cudaSuccess)
+            return CO_ERR_CUDA;
+    }
+    int grid = red_blocks(c, N);
+    int cap = max_blocks_per_sm * c->nsm;
+    if (grid > cap) grid = cap;
+    if (grid > c->mb.red_cap / 2) grid = c->mb.red_cap / 2;
+    if (grid < 1) grid = 1;
+    unsigned *bar = (unsigned *)(c->mb.red + (size_t)c->mb.red_cap * CO_RED_COMPS);
+    int *err = (int *)(bar + 4);
+    CO_CK(cudaMemsetAsync(bar, 0, 32, c->stream));
+    double *red7 = c->mb.red + (size_t)c->mb.red_cap * 8;  // disjoint from red2 (first 2*grid)
+    double *red2 = c->mb.red;
+    int use_lambda = gonzalez;
+    void *args[] = {&N, &vmid, &w, &g, &dv, &use_lambda, &nu, &dt, &v0, &Gv, &v1, &r,
+                    &red7, &red2, &c->st, &bar, &err};
+    CO_CK(cudaLaunchCooperativeKernel((void *)k_lb_fused, grid, CO_RED_THREADS, args, 0,
+                                      c->stream));
+    c->launches++;
+    return CO_OK;
+}
+
+// One Picard map on device buffers. vin/v0/w device pointers (w must be
+// c->mb.w). If r != nullptr, r = Gv - vin with residual partials in mb.red.
+static int picard_map_impl(co_ctx *c, int model, int gonzalez, double nu, int precision,
+                           double *Gv, const double *vin, const double *v0, int N, double S0,
+                           double dt, double *r, int *nred_out) {
+    int rc;
+    co_bufs &b = c->mb;
+    int nred = red_blocks(c, N);
+    if (gonzalez)
+        if ((rc = entropy_into_state(c, vin, N))) return rc;
+    if ((rc = co_mid_dv(c, vin, v0, N))) return rc;
+    if ((rc = co_sort_markers(c, b.vmid, N))) return rc;
+    if ((rc = co_project_sorted(c, c->f))) return rc;
+    if (model == CO_MODEL_LB) {
+        if ((rc = co_loggrad_dev(c, b.vmid, N, c->f, b.G, b.w, b.dv, b.red))) return rc;
+        k_lambda<<<1, 256, 0, c->stream>>>(b.red, nred, c->st, S0, gonzalez);
+        c->launches++;
+        CO_CK(cudaGetLastError());
+        if ((rc = co_lb_fused(c, N, nu, dt, Gv, v0, b.vmid, b.w, b.G, b.dv, gonzalez, vin, r)))
+            return rc;
+        // residual partials of the fused kernel use its own grid size
+        int max_bps = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_bps, k_lb_fused, CO_RED_THREADS, 0);
+        int grid = red_blocks(c, N);
+        if (grid > max_bps * c->nsm) grid = max_bps * c->nsm;
+        if (grid > c->mb.red_cap / 2) grid = c->mb.red_cap / 2;
+        if (grid < 1) grid = 1;
+        nred = grid;
+    } else {
+        if ((rc = co_compute_r_dev(c, c->f, c->rr))) return rc;
+        if ((rc = co_mass_solve_dev(c, c->rr, c->L))) return rc;
+        if ((rc = co_grad_L_dev(c, b.vmid, N, c->L, b.G, b.w, b.dS, b.dv, b.red))) return rc;
+        k_lambda<<<1, 256, 0, c->stream>>>(b.red, nred, c->st, S0, gonzalez);
+        c->launches++;
+        CO_CK(cudaGetLastError());
+        if ((rc = co_pack_landau(c, N, N, precision, gonzalez))) return rc;
+        if (precision == CO_PREC_MIXED)
+            rc = co_pair_fp32(c, N);
+        else
+            rc = co_pair_fp64(c, N, 0);
+        if (rc) return rc;
+        if ((rc = co_unpack_update(c, N, dt, Gv, v0, vin, r, r ? b.red : nullptr))) return rc;
+    }
+    if (nred_out) *nred_out = nred;
+    return CO_OK;
+}
+
+int co_picard_map_dev(co_ctx *c, const co_opts *o, int precision, double *Gv,
+                      const double *vin, const double *v0, const double *w, int N, double S0,
+                      double dt, int want_resid) {
+    (void)w;
+    return picard_map_impl(c, o->model, o->use_gonzalez, o->nu, precision, Gv, vin, v0, N, S0,
+                           dt, want_resid ? c->mb.r : nullptr, nullptr);
+}
+
+static co_dev_opts dev_opts(const co_opts *o, double floor_extra) {
+    co_dev_opts d;
+    d.use_anderson = o->use_anderson;
+    d.exit_picard_step = o->exit_picard_step;
+    d.m = o->m;
+    d.max_iter = o->max_iter;
+    d.stag_window = o->stag_window;
+    d.damp_decay_start = o->damp_decay_start;
+    d.tol = o->tol;
+    d.abs_floor = fmax(o->abs_floor, floor_extra);
+    d.stag_rel_tol = o->stag_rel_tol;
+    d.damp_decay_factor = o->damp_decay_factor;
+    d.restart_factor = o->restart_factor;
+    d.damping = o->damping;
+    d.reg_factor = o->reg_factor;
+    return d;
+}
+
+// The Anderson loop on device buffers mb.v1 (in/out), mb.v0, mb.w.
+// precision selects the pair kernel of the maps.
+static int anderson_loop(co_ctx *c, const co_opts *o, int precision, int N, double S0, double dt,
+                         co_dev_opts d, int max_iter, int *iters_out) {
+    int rc;
+    co_bufs &b = c->mb;
+    int n2 = 2 * N;
+    size_t ldF = 2 * (size_t)b.cap;
+    int eg = ew_grid(c, n2);
+    k_state_reset<<<1, 32, 0, c->stream>>>(c->st);
+    c->launches++;
+    int k;
+    for (k = 1; k <= max_iter; k++) {
+        int nred = 0;
+        if ((rc = picard_map_impl(c, o->model, o->use_gonzalez, o->nu, precision, b.Gv, b.v1,
+                                  b.v0, N, S0, dt, b.r, &nred)))
+            return rc;
+        k_ctrl1<<<1, 256, 0, c->stream>>>(b.red, nred, c->st, d);
+        k_plain_update<<<eg, 256, 0, c->stream>>>(n2, c->st, o->exit_picard_step, b.v1, b.Gv, b.r,
+                                                  b.rp, b.Gp, b.vbest);
+        c->launches += 2;
+        if (o->use_anderson) {
+            int ng = red_blocks(c, n2);
+            k_anderson_cols<<<ng, CO_RED_THREADS, 0, c->stream>>>(n2, c->st, b.r, b.rp, b.Gv, b.Gp,
+                                                                  b.dF, b.dG, ldF, b.red);
+            k_anderson_solve<<<1, 256, 0, c->stream>>>(b.red, ng, c->st, d);
+            k_anderson_update<<<eg, 256, 0, c->stream>>>(n2, c->st, b.v1, b.Gv, b.dG, ldF);
+            c->launches += 3;
+        }
+        CO_CK(cudaGetLastError());
+        CO_CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(co_solver_state), cudaMemcpyDeviceToHost,
+                              c->stream));
+        CO_CK(cudaStreamSynchronize(c->stream));
+        if (c->st_host->done) break;
+    }
+    if (k > max_iter) {
+        k_set_done<<<1, 32, 0, c->stream>>>(c->st, 3);
+        c->launches++;
+    }
+    k_finish<<<eg, 256, 0, c->stream>>>(n2, c->st, o->exit_picard_step, b.v1, b.Gv, b.vbest);
+    c->launches++;
+    CO_CK(cudaGetLastError());
+    CO_CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(co_solver_state), cudaMemcpyDeviceToHost,
+                          c->stream));
+    CO_CK(cudaStreamSynchronize(c->stream));
+    if (iters_out) *iters_out = k > max_iter ? max_iter : k;
+    if (c->st_host->error) return c->st_host->error;
+    return CO_OK;
+}
+
+// step_anderson! on device buffers: mb.v1 (guess in, solution out), mb.v0, mb.w
+int co_step_anderson_buffers(co_ctx *c, const co_opts *o, int N, double S0, double dt,
+                             int *iters, double *res, int *nrs, double *r0) {
+    int rc;
+    if (o->m < 1 || o->m > CO_MAX_M) return CO_ERR_ARG;
+    if ((rc = co_ensure_capacity(c, N, o->m))) return rc;
+    if (N == 0) {
+        if (iters) *iters = 0;
+        if (res) *res = 0;
+        if (nrs) *nrs = 0;
+        if (r0) *r0 = 0;
+        return CO_OK;
+    }
+    int it = 0;
+    if (o->precision == CO_PREC_MIXED) {
+        // phase 1: Anderson on the FP32-pair map, floored at mixed_floor
+        double fl = o->mixed_floor > 0 ? o->mixed_floor : 0.0;
+        co_dev_opts d = dev_opts(o, fl);
+        if ((rc = anderson_loop(c, o, CO_PREC_MIXED, N, S0, dt, d, o->max_iter, &it))) return rc;
+        double r0_32 = c->st_host->nrm_r0;
+        int nrs32 = c->st_host->n_restart;
+        // phase 2: the FP64 exit Picard map G64(v) (exit_picard_step)
+        co_bufs &b = c->mb;
+        int nred = 0;
+        if ((rc = picard_map_impl(c, o->model, o->use_gonzalez, o->nu, CO_PREC_FP64, b.Gv, b.v1,
+                                  b.v0, N, S0, dt, b.r, &nred)))
+            return rc;
+        co_dev_opts d64 = dev_opts(o, 0.0);
+        d64.max_iter = 1;
+        k_state_reset<<<1, 32, 0, c->stream>>>(c->st);
+        k_ctrl1<<<1, 256, 0, c->stream>>>(b.red, nred, c->st, d64);
+        c->launches += 2;
+        CO_CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(co_solver_state), cudaMemcpyDeviceToHost,
+                              c->stream));
+        CO_CK(cudaStreamSynchronize(c->stream));
+        if (c->st_host->error) return c->st_host->error;
+        if (o->exit_picard_step)
+            CO_CK(cudaMemcpyAsync(b.v1, b.Gv, 2 * (size_t)N * sizeof(double),
+                                  cudaMemcpyDeviceToDevice, c->stream));
+        CO_CK(cudaStreamSynchronize(c->stream));
+        if (iters) *iters = it + 1;
+        if (res) *res = c->st_host->nrm_r;
+        if (nrs) *nrs = nrs32;
+        if (r0) *r0 = r0_32;
+        return CO_OK;
+    }
+    co_dev_opts d = dev_opts(o, 0.0);
+    if ((rc = anderson_loop(c, o, CO_PREC_FP64, N, S0, dt, d, o->max_iter, &it))) return rc;
+    if (iters) *iters = c->st_host->done == 0 || c->st_host->done == 3 ? o->max_iter : c->st_host->k;
+    if (res) *res = c->st_host->res_out;
+    if (nrs) *nrs = c->st_host->n_restart;
+    if (r0) *r0 = c->st_host->nrm_r0;
+    return CO_OK;
+}
+
+// Explicit predictor (main.jl:233-245) on device: out = v + dt vdot(v)
+int co_predictor_buffers(co_ctx *c, const co_opts *o, int precision, const double *v, int N,
+                         double dt, double *out) {
+    int rc;
+    co_bufs &b = c->mb;
+    if ((rc = co_ensure_capacity(c, N, 1))) return rc;
+    if (N == 0) return CO_OK;
+    if ((rc = co_sort_markers(c, v, N))) return rc;
+    if ((rc = co_project_sorted(c, c->f))) return rc;
+    if (o->model == CO_MODEL_LB) {
+        if ((rc = co_loggrad_dev(c, v, N, c->f, b.G, b.w, nullptr, nullptr))) return rc;
+        if ((rc = co_lb_fused(c, N, o->nu, dt, out, v, v, b.w, b.G, nullptr, 0, nullptr, nullptr)))
+            return rc;
+    } else {
+        if ((rc = co_compute_r_dev(c, c->f, c->rr))) return rc;
+        if ((rc = co_mass_solve_dev(c, c->rr, c->L))) return rc;
+        if ((rc = co_grad_L_dev(c, v, N, c->L, b.G, nullptr, nullptr, nullptr, nullptr))) return rc;
+        if ((rc = co_pack_plain(c, N, N, precision, v, b.G))) return rc;
+        rc = precision == CO_PREC_MIXED ? co_pair_fp32(c, N) : co_pair_fp64(c, N, 0);
+        if (rc) return rc;
+        if ((rc = co_unpack_update(c, N, dt, out, v, nullptr, nullptr, nullptr))) return rc;
+    }
+    CO_CK(cudaGetLastError());
+    return CO_OK;
+}

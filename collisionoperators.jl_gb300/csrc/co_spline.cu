@@ -1,0 +1,610 @@
+// co_spline.cu -- the P_DEG=2 particle <-> spline stage on the device.
+//
+// Replaces projection_gpu.jl (atomic scatter, gathers) and the CPU parts of
+// the chain (mass solve, quadrature) with deterministic kernels:
+//   1. locate:   cell id and reference coordinates per marker, per-chunk cell
+//                histograms (integer, so order-independent);
+//   2. sort:     stable counting sort of the in-domain markers by cell
+//                (chunk-major offsets + warp-sequential ranks), which also
+//                compacts away out-of-domain markers;
+//   3. scatter:  b = sum_a w_a phi_k(v_a) as a segmented sum per (cell, local
+//                basis) in marker order, then a fixed 3x3-cell gather per dof;
+//   4. solve:    M = M1 (x) M2 (tensor-product mass matrix), so M^{-1} b is two
+//                small dense products with the 1D inverses;
+//   5. quadrature for r (functions.jl:158-179) and S (functions.jl:137-155),
+//                one block per element, fixed-order reductions;
+//   6. gathers:  grad L (functions.jl:182-202) and the clamped log-gradient
+//                (functions.jl:37-64) per marker.
+// Everything is FP64 and bitwise reproducible run to run.
+#include "co_internal.cuh"
+#include "co_reduce.cuh"
+
+// ---------------------------------------------------------------- basis
+
+// _bernstein_eval! for p = 2 (MantisWrappers.jl:201-216), same expressions.
+__device__ __forceinline__ void bern2(double xi, double *B, double *dB) {
+    double om = 1.0 - xi;
+    B[0] = om * om;
+    B[1] = 2.0 * xi * om;
+    B[2] = xi * xi;
+    if (dB) {
+        dB[0] = 2.0 * (0.0 - om);
+        dB[1] = 2.0 * (om - xi);
+        dB[2] = 2.0 * xi;
+    }
+}
+
+// phi[j] = sum_k C[k][j] B[k]  (mul!(phi, transpose(C), B))
+__device__ __forceinline__ void extract3(const double *__restrict__ c, const double *B,
+                                         double *phi) {
+#pragma unroll
+    for (int j = 0; j < 3; j++) phi[j] = c[0 * 3 + j] * B[0] + c[1 * 3 + j] * B[1] + c[2 * 3 + j] * B[2];
+}
+
+// searchsortedlast - 1 on bp[0..n] for bp[0] < x < bp[n] (_cell_search,
+// projection_gpu.jl:20-32)
+__device__ __forceinline__ int cell_search(const double *__restrict__ bp, int n, double x) {
+    int lo = 0, hi = n;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (bp[mid] <= x) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// ---------------------------------------------------------------- kernels
+
+// v_mid = 0.5 (v0 + v_in), dv = v_in - v0  (solver.jl:181-182)
+__global__ void k_mid_dv(const double *__restrict__ vin, const double *__restrict__ v0,
+                         double *__restrict__ vmid, double *__restrict__ dv, int n2) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n2) {
+        double a = vin[i], b = v0[i];
+        vmid[i] = 0.5 * (b + a);
+        dv[i] = a - b;
+    }
+}
+
+// locate_particle (MantisWrappers.jl:168-179) + per-chunk cell histogram.
+__global__ void __launch_bounds__(CO_CHUNK)
+k_locate_hist(const double *__restrict__ x, int N, const double *__restrict__ bp1, int n1,
+              const double *__restrict__ bp2, int n2, int *__restrict__ cell,
+              double *__restrict__ xi, int *__restrict__ hist, int n_el) {
+    extern __shared__ int hs[];
+    for (int i = threadIdx.x; i < n_el; i += blockDim.x) hs[i] = 0;
+    __syncthreads();
+    int a = blockIdx.x * CO_CHUNK + threadIdx.x;
+    if (a < N) {
+        double v1 = x[a], v2 = x[N + a];
+        int c = -1;
+        double x1 = 0.0, x2 = 0.0;
+        if (!(v1 <= bp1[0] || v1 >= bp1[n1] || v2 <= bp2[0] || v2 >= bp2[n2])) {
+            int i = cell_search(bp1, n1, v1);
+            int j = cell_search(bp2, n2, v2);
+            x1 = (v1 - bp1[i]) / (bp1[i + 1] - bp1[i]);
+            x2 = (v2 - bp2[j]) / (bp2[j + 1] - bp2[j]);
+            c = i + j * n1;
+            atomicAdd(&hs[c], 1);
+        }
+        cell[a] = c;
+        xi[a] = x1;
+        xi[N + a] = x2;
+    }
+    __syncthreads();
+    if (hist)
+        for (int i = threadIdx.x; i < n_el; i += blockDim.x)
+            hist[(size_t)blockIdx.x * n_el + i] = hs[i];
+}
+
+// per cell: exclusive offsets of each chunk within the cell, and the count
+__global__ void k_cellcount(const int *__restrict__ hist, int nchunk, int n_el,
+                            int *__restrict__ hoff, int *__restrict__ count) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n_el) return;
+    int run = 0;
+    for (int k = 0; k < nchunk; k++) {
+        int h = hist[(size_t)k * n_el + c];
+        hoff[(size_t)k * n_el + c] = run;
+        run += h;
+    }
+    count[c] = run;
+}
+
+// exclusive scan of count[0..n) -> cstart[0..n]; one block of 1024 threads
+__global__ void __launch_bounds__(1024)
+k_cellscan(const int *__restrict__ count, int n, int *__restrict__ cstart) {
+    __shared__ int sh[1024];
+    int per = (n + 1023) / 1024;
+    int t = threadIdx.x;
+    int b0 = t * per, b1 = min(n, b0 + per);
+    int s = 0;
+    for (int i = b0; i < b1; i++) s += count[i];
+    sh[t] = s;
+    __syncthreads();
+    // Hillis-Steele inclusive scan of the 1024 thread sums
+    for (int o = 1; o < 1024; o <<= 1) {
+        int v = t >= o ? sh[t - o] : 0;
+        __syncthreads();
+        sh[t] += v;
+        __syncthreads();
+    }
+    int run = t > 0 ? sh[t - 1] : 0;
+    for (int i = b0; i < b1; i++) {
+        cstart[i] = run;
+        run += count[i];
+    }
+    if (t == 1023) cstart[n] = sh[1023];
+}
+
+// Stable placement: rank of each marker among the markers of its cell that
+// precede it in its chunk, warps taking turns in index order.
+__global__ void __launch_bounds__(CO_CHUNK)
+k_perm(const int *__restrict__ cell, int N, const int *__restrict__ hoff,
+       const int *__restrict__ cstart, int n_el, int n1, const double *__restrict__ w,
+       const double *__restrict__ xi, const double *__restrict__ C1,
+       const double *__restrict__ C2, int *__restrict__ perm, int *__restrict__ inv,
+       int *__restrict__ scell, double *__restrict__ sw, double *__restrict__ sphi) {
+    extern __shared__ int run[];
+    for (int i = threadIdx.x; i < n_el; i += blockDim.x) run[i] = 0;
+    __syncthreads();
+    int a = blockIdx.x * CO_CHUNK + threadIdx.x;
+    int c = a < N ? cell[a] : -2;
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned peers = __match_any_sync(0xffffffffu, c);
+    int rank = __popc(peers & ((1u << lane) - 1u));
+    int leader = __ffs(peers) - 1;
+    int base = 0;
+    for (int wv = 0; wv < (CO_CHUNK >> 5); wv++) {
+        if (warp == wv) {
+            int b = 0;
+            if (c >= 0 && lane == leader) {
+                b = run[c];
+                run[c] = b + __popc(peers);
+            }
+            base = __shfl_sync(0xffffffffu, b, leader);
+        }
+        __syncthreads();
+    }
+    if (a >= N) return;
+    if (c < 0) {
+        inv[a] = -1;
+        return;
+    }
+    int pos = cstart[c] + hoff[(size_t)blockIdx.x * n_el + c] + base + rank;
+    perm[pos] = a;
+    inv[a] = pos;
+    scell[pos] = c;
+    sw[pos] = w[a];
+    if (sphi) {
+        int i = c % n1, j = c / n1;
+        double B[3], p[3];
+        bern2(xi[a], B, nullptr);
+        extract3(C1 + 9 * i, B, p);
+        double *o = sphi + (size_t)pos * 6;
+        o[0] = p[0]; o[1] = p[1]; o[2] = p[2];
+        bern2(xi[N + a], B, nullptr);
+        extract3(C2 + 9 * j, B, p);
+        o[3] = p[0]; o[4] = p[1]; o[5] = p[2];
+    }
+}
+
+// segmented sum per (cell, local basis j1 + 3 j2) in marker order
+__global__ void k_cellsum(const int *__restrict__ cstart, const double *__restrict__ sw,
+                          const double *__restrict__ sphi, int n_el, double *__restrict__ bS) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_el * 9) return;
+    int c = t / 9, j = t - 9 * c;
+    int j1 = j % 3, j2 = j / 3;
+    int p0 = cstart[c], p1 = cstart[c + 1];
+    double acc = 0.0;
+    for (int p = p0; p < p1; p++) {
+        const double *ph = sphi + (size_t)p * 6;
+        double val = ph[j1] * ph[3 + j2];
+        acc += sw[p] * val;
+    }
+    bS[t] = acc;
+}
+
+// dof k = (k1, k2) gathers the <= 9 cell-local entries that touch it
+__global__ void k_dofgather(const double *__restrict__ src, int n1, int n2, int nd1, int nd2,
+                            double *__restrict__ out) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nd1 * nd2) return;
+    int k1 = k % nd1, k2 = k / nd1;
+    double acc = 0.0;
+    for (int b = 0; b < 3; b++) {
+        int jj = k2 - b;
+        if (jj < 0 || jj >= n2) continue;
+        for (int a = 0; a < 3; a++) {
+            int i = k1 - a;
+            if (i < 0 || i >= n1) continue;
+            acc += src[(size_t)(i + jj * n1) * 9 + a + 3 * b];
+        }
+    }
+    out[k] = acc;
+}
+
+// y[:, i2] = M1^{-1} b[:, i2]
+__global__ void k_mass1(const double *__restrict__ Minv1, const double *__restrict__ b, int nd1,
+                        int nd2, double *__restrict__ y) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nd1 * nd2) return;
+    int i1 = t % nd1, i2 = t / nd1;
+    const double *row = Minv1 + (size_t)i1 * nd1;
+    const double *col = b + (size_t)i2 * nd1;
+    double s = 0.0;
+    for (int k = 0; k < nd1; k++) s = fma(row[k], col[k], s);
+    y[t] = s;
+}
+
+// out[i1, :] = y[i1, :] M2^{-1}
+__global__ void k_mass2(const double *__restrict__ Minv2, const double *__restrict__ y, int nd1,
+                        int nd2, double *__restrict__ out) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nd1 * nd2) return;
+    int i1 = t % nd1, i2 = t / nd1;
+    double s = 0.0;
+    for (int k = 0; k < nd2; k++) s = fma(y[(size_t)k * nd1 + i1], Minv2[(size_t)k * nd2 + i2], s);
+    out[t] = s;
+}
+
+// One block per element: f at the nq x nq Gauss points, then r-local (mode 0)
+// or the entropy partial (mode 1).
+__global__ void __launch_bounds__(64)
+k_elem(const double *__restrict__ fc, int n1, int n2, int nd1, int nq,
+       const double *__restrict__ Tq1, const double *__restrict__ Tq2,
+       const double *__restrict__ qw, const double *__restrict__ bp1,
+       const double *__restrict__ bp2, int logsq, int mode, double *__restrict__ E,
+       double *__restrict__ Ep) {
+    __shared__ double contrib[64 * 9];
+    __shared__ double cs[9];
+    int e = blockIdx.x;
+    int i = e % n1, j = e / n1;
+    int t = threadIdx.x;
+    if (t < 9) cs[t] = fc[(i + t % 3) + (j + t / 3) * nd1];
+    __syncthreads();
+    int nqq = nq * nq;
+    double jac = (bp1[i + 1] - bp1[i]) * (bp2[j + 1] - bp2[j]);
+    if (t < nqq) {
+        int q1 = t % nq, q2 = t / nq;
+        double p1[3], p2[3], phi[9];
+        for (int a = 0; a < 3; a++) {
+            p1[a] = Tq1[((size_t)i * 3 + a) * nq + q1];
+            p2[a] = Tq2[((size_t)j * 3 + a) * nq + q2];
+        }
+        double f = 0.0;
+        for (int b = 0; b < 3; b++)
+            for (int a = 0; a < 3; a++) {
+                phi[a + 3 * b] = p1[a] * p2[b];
+                f += cs[a + 3 * b] * phi[a + 3 * b];
+            }
+        double wq = qw[q1] * qw[q2];
+        if (mode == 0) {
+            double integrand;
+            if (logsq)
+                integrand = f * f > 1e-60 ? (1 + 0.5 * log(f * f)) : 0.0;
+            else
+                integrand = f > 1e-30 ? (1 + log(f)) : 0.0;
+            for (int k = 0; k < 9; k++) contrib[t * 9 + k] = integrand * phi[k] * wq * jac;
+        } else {
+            double s = 0.0;
+            if (logsq) {
+                if (f * f > 1e-60) s = -(f * 0.5 * log(f * f) * wq * jac);
+            } else if (f > 1e-30) {
+                s = -(f * log(f) * wq * jac);
+            }
+            contrib[t] = s;
+        }
+    }
+    __syncthreads();
+    if (mode == 0) {
+        if (t < 9) {
+            double s = 0.0;
+            for (int q = 0; q < nqq; q++) s += contrib[q * 9 + t];
+            E[(size_t)e * 9 + t] = s;
+        }
+    } else if (t == 0) {
+        double s = 0.0;
+        for (int q = 0; q < nqq; q++) s += contrib[q];
+        Ep[e] = s;
+    }
+}
+
+// S = sum_e Ep[e] in a fixed order (one block)
+__global__ void __launch_bounds__(256)
+k_sum_to(const double *__restrict__ Ep, int n, double *__restrict__ out) {
+    __shared__ double sh[32];
+    double s = co_sum_partials(Ep, n, 1, 0, sh);
+    if (threadIdx.x == 0) *out = s;
+}
+
+// compute_G! (functions.jl:182-202) at markers x, optionally with dS = -w G
+// (solver.jl:69-72) and the Gonzalez partials dv.dS, |dv|^2 (solver.jl:98-103).
+__global__ void __launch_bounds__(CO_RED_THREADS)
+k_grad_L(const double *__restrict__ x, int N, const int *__restrict__ cell,
+         const double *__restrict__ xi, const double *__restrict__ Lc, int n1, int nd1,
+         const double *__restrict__ bp1, const double *__restrict__ bp2,
+         const double *__restrict__ C1, const double *__restrict__ C2,
+         double *__restrict__ G, const double *__restrict__ w, double *__restrict__ dS,
+         const double *__restrict__ dv, double *__restrict__ red) {
+    __shared__ double sh[32];
+    double pdot = 0.0, pn2 = 0.0;
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < N; a += gridDim.x * blockDim.x) {
+        int c = cell[a];
+        double acc1 = 0.0, acc2 = 0.0;
+        if (c >= 0) {
+            int i = c % n1, j = c / n1;
+            double h1 = bp1[i + 1] - bp1[i], h2 = bp2[j + 1] - bp2[j];
+            double ih1 = 1.0 / h1, ih2 = 1.0 / h2;
+            double B1[3], dB1[3], B2[3], dB2[3], p1[3], dp1[3], p2[3], dp2[3];
+            bern2(xi[a], B1, dB1);
+            bern2(xi[N + a], B2, dB2);
+            extract3(C1 + 9 * i, B1, p1);
+            extract3(C1 + 9 * i, dB1, dp1);
+            extract3(C2 + 9 * j, B2, p2);
+            extract3(C2 + 9 * j, dB2, dp2);
+            for (int b = 0; b < 3; b++)
+                for (int q = 0; q < 3; q++) {
+                    double Lv = Lc[(i + q) + (j + b) * nd1];
+                    acc1 += Lv * (dp1[q] * p2[b]) * ih1;
+                    acc2 += Lv * (p1[q] * dp2[b]) * ih2;
+                }
+        }
+        G[a] = acc1;
+        G[N + a] = acc2;
+        if (dS) {
+            double s1 = -w[a] * acc1, s2 = -w[a] * acc2;
+            dS[a] = s1;
+            dS[N + a] = s2;
+            if (red) {
+                double d1 = dv[a], d2 = dv[N + a];
+                pdot += d1 * s1 + d2 * s2;
+                pn2 += d1 * d1 + d2 * d2;
+            }
+        }
+    }
+    if (red) {
+        double s = co_block_sum(pdot, sh);
+        double n = co_block_sum(pn2, sh);
+        if (threadIdx.x == 0) {
+            red[blockIdx.x * 2 + 0] = s;
+            red[blockIdx.x * 2 + 1] = n;
+        }
+    }
+}
+
+// eval_loggrad_at_particles! (functions.jl:37-64) with the LB Gonzalez partials
+// -sum w dv.g and |dv|^2 (solver.jl:198-203).
+__global__ void __launch_bounds__(CO_RED_THREADS)
+k_loggrad(const double *__restrict__ x, int N, const int *__restrict__ cell,
+          const double *__restrict__ xi, const double *__restrict__ fc, int n1, int nd1,
+          const double *__restrict__ bp1, const double *__restrict__ bp2,
+          const double *__restrict__ C1, const double *__restrict__ C2,
+          double *__restrict__ g, const double *__restrict__ w,
+          const double *__restrict__ dv, double *__restrict__ red) {
+    __shared__ double sh[32];
+    double pdot = 0.0, pn2 = 0.0;
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < N; a += gridDim.x * blockDim.x) {
+        int c = cell[a];
+        double g1 = 0.0, g2 = 0.0;
+        if (c >= 0) {
+            int i = c % n1, j = c / n1;
+            double h1 = bp1[i + 1] - bp1[i], h2 = bp2[j + 1] - bp2[j];
+            double ih1 = 1.0 / h1, ih2 = 1.0 / h2;
+            double B1[3], dB1[3], B2[3], dB2[3], p1[3], dp1[3], p2[3], dp2[3];
+            bern2(xi[a], B1, dB1);
+            bern2(xi[N + a], B2, dB2);
+            extract3(C1 + 9 * i, B1, p1);
+            extract3(C1 + 9 * i, dB1, dp1);
+            extract3(C2 + 9 * j, B2, p2);
+            extract3(C2 + 9 * j, dB2, dp2);
+            double f = 0.0, d1 = 0.0, d2 = 0.0;
+            for (int b = 0; b < 3; b++)
+                for (int q = 0; q < 3; q++) {
+                    double cv = fc[(i + q) + (j + b) * nd1];
+                    f += cv * (p1[q] * p2[b]);
+                    d1 += cv * (dp1[q] * p2[b]) * ih1;
+                    d2 += cv * (p1[q] * dp2[b]) * ih2;
+                }
+            double invf = 1.0 / fmax(fabs(f), CO_FS_FLOOR);
+            g1 = fmin(fmax(d1 * invf, -CO_G_MAX), CO_G_MAX);
+            g2 = fmin(fmax(d2 * invf, -CO_G_MAX), CO_G_MAX);
+        }
+        g[a] = g1;
+        g[N + a] = g2;
+        if (red) {
+            double e1 = dv[a], e2 = dv[N + a];
+            pdot -= w[a] * (e1 * g1 + e2 * g2);
+            pn2 += e1 * e1 + e2 * e2;
+        }
+    }
+    if (red) {
+        double s = co_block_sum(pdot, sh);
+        double n = co_block_sum(pn2, sh);
+        if (threadIdx.x == 0) {
+            red[blockIdx.x * 2 + 0] = s;
+            red[blockIdx.x * 2 + 1] = n;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- host side
+
+int co_mid_dv(co_ctx *c, const double *vin, const double *v0, int N) {
+    if (N == 0) return CO_OK;
+    k_mid_dv<<<co_cdiv(2LL * N, 256), 256, 0, c->stream>>>(vin, v0, c->mb.vmid, c->mb.dv, 2 * N);
+    c->launches++;
+    CO_CK(cudaGetLastError());
+    return CO_OK;
+}
+
+// locate + stable sort of markers x (N). Results: mb.cell, mb.xi, mb.perm,
+// mb.inv, mb.scell, mb.sw, mb.sphi, cstart (M_in = cstart[n_el] on device).
+int co_sort_markers(co_ctx *c, const double *x, int N) {
+    co_bufs &b = c->mb;
+    int nchunk = co_cdiv(N, CO_CHUNK);
+    if (nchunk == 0) nchunk = 1;
+    size_t sm = sizeof(int) * (size_t)c->n_el;
+    if (N > 0) {
+        k_locate_hist<<<nchunk, CO_CHUNK, sm, c->stream>>>(x, N, c->bp1, c->n1, c->bp2, c->n2,
+                                                          b.cell, b.xi, b.hist, c->n_el);
+        c->launches++;
+    } else {
+        CO_CK(cudaMemsetAsync(b.hist, 0, sizeof(int) * c->n_el, c->stream));
+    }
+    k_cellcount<<<co_cdiv(c->n_el, 256), 256, 0, c->stream>>>(b.hist, N > 0 ? nchunk : 1,
+                                                              c->n_el, b.hoff, b.count);
+    k_cellscan<<<1, 1024, 0, c->stream>>>(b.count, c->n_el, b.cstart);
+    c->launches += 2;
+    if (N > 0) {
+        k_perm<<<nchunk, CO_CHUNK, sm, c->stream>>>(b.cell, N, b.hoff, b.cstart, c->n_el, c->n1,
+                                                   b.w, b.xi, c->C1, c->C2, b.perm, b.inv,
+                                                   b.scell, b.sw, b.sphi);
+        c->launches++;
+    }
+    CO_CK(cudaGetLastError());
+    return CO_OK;
+}
+
+int co_mass_solve_dev(co_ctx *c, const double *rhs, double *out) {
+    int n = c->n_dofs;
+    k_mass1<<<co_cdiv(n, 128), 128, 0, c->stream>>>(c->Minv1, rhs, c->nd1, c->nd2, c->y);
+    k_mass2<<<co_cdiv(n, 128), 128, 0, c->stream>>>(c->Minv2, c->y, c->nd1, c->nd2, out);
+    c->launches += 2;
+    CO_CK(cudaGetLastError());
+    return CO_OK;
+}
+
+// after co_sort_markers: b = scatter, f = M^{-1} b
+int co_project_sorted(co_ctx *c, double *f_out) {
+    int t = c->n_el * 9;
+    k_cellsum<<<co_cdiv(t, 128), 128, 0, c->stream>>>(c->mb.cstart, c->mb.sw, c->mb.sphi,
+                                                      c->n_el, c->bS);
+    k_dofgather<<<co_cdiv(c->n_dofs, 128), 128, 0, c->stream>>>(c->bS, c->n1, c->n2, c->nd1,
+                                                                c->nd2, c->b);
+    c->launches += 2;
+    CO_CK(cudaGetLastError());
+    return co_mass_solve_dev(c, c->b, f_out);
+}
+
+int co_compute_r_dev(co_ctx *c, const double *f, double *r) {
+    k_elem<<<c->n_el, 64, 0, c->stream>>>(f, c->n1, c->n2, c->nd1, c->nq, c->Tq1, c->Tq2, c->qw,
+                                          c->bp1, c->bp2, (c->flags & CO_FLAG_LOGSQ) ? 1 : 0, 0,
+                                          c->E, nullptr);
+    k_dofgather<<<co_cdiv(c->n_dofs, 128), 128, 0, c->stream>>>(c->E, c->n1, c->n2, c->nd1,
+                                                                c->nd2, r);
+    c->launches += 2;
+    CO_CK(cudaGetLastError());
+    return CO_OK;
+}
+
+int co_entropy_parts_dev(co_ctx *c, const double *f) {
+    k_elem<<<c->n_el, 64, 0, c->stream>>>(f, c->n1, c->n2, c->nd1, c->nq, c->Tq1, c->Tq2, c->qw,
+                                          c->bp1, c->bp2, (c->flags & CO_FLAG_LOGSQ) ? 1 : 0, 1,
+                                          nullptr, c->Ep);
+    c->launches++;
+    CO_CK(cudaGetLastError());
+    return CO_OK;
+}
+
+int co_entropy_finalize_dev(co_ctx *c, double *S_dev) {
+    k_sum_to<<<1, 256, 0, c->stream>>>(c->Ep, c->n_el, S_dev);
+    c->launches++;
+    CO_CK(cudaGetLastError());
+    return CO_OK;
+}
+
+static int red_grid(co_ctx *c, int N) {
+    int g = co_cdiv(N, CO_RED_THREADS);
+    if (g > c->mb.red_cap) g = c->mb.red_cap;
+    if (g < 1) g = 1;
+    return g;
+}
+
+// gradient gather at x (cell/xi from the last locate of x)
+int co_grad_L_dev(co_ctx *c, const double *x, int N, const double *L, double *G,
+                  const double *w, double *dS, const double *dv, double *red) {
+    if (N == 0) return CO_OK;
+    k_grad_L<<<red_grid(c, N), CO_RED_THREADS, 0, c->stream>>>(
+        x, N, c->mb.cell, c->mb.xi, L, c->n1, c->nd1, c->bp1, c->bp2, c->C1, c->C2, G, w, dS, dv,
+        red);
+    c->launches++;
+    CO_CK(cudaGetLastError());
+    return CO_OK;
+}
+
+int co_loggrad_dev(co_ctx *c, const double *x, int N, const double *f, double *g,
+                   const double *w, const double *dv, double *red) {
+    if (N == 0) return CO_OK;
+    k_loggrad<<<red_grid(c, N), CO_RED_THREADS, 0, c->stream>>>(
+        x, N, c->mb.cell, c->mb.xi, f, c->n1, c->nd1, c->bp1, c->bp2, c->C1, c->C2, g, w, dv, red);
+    c->launches++;
+    CO_CK(cudaGetLastError());
+    return CO_OK;
+}
+
+// dynamic shared memory of the sort kernels (one int per cell)
+int co_spline_configure(co_ctx *c) {
+    int bytes = (int)(sizeof(int) * (size_t)c->n_el);
+    if (bytes > 48 * 1024) {
+        if (bytes > 200 * 1024) return CO_ERR_UNSUPPORTED;
+        CO_CK(cudaFuncSetAttribute(k_locate_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        CO_CK(cudaFuncSetAttribute(k_perm, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    }
+    return CO_OK;
+}
+
+// ------------------------------------------------------------- capacity
+
+template <typename T>
+static int grow(T **p, size_t n) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    if (n == 0) n = 1;
+    if (cudaMalloc((void **)p, n * sizeof(T)) != cudaSuccess) return CO_ERR_NOMEM;
+    return CO_OK;
+}
+
+int co_ensure_capacity(co_ctx *c, int N, int m) {
+    co_bufs &b = c->mb;
+    int rc;
+    if (N > b.cap) {
+        int cap = N < 1024 ? 1024 : N;
+        size_t n2 = 2 * (size_t)cap;
+        double **d2[] = {&b.vmid, &b.dv, &b.G, &b.dS, &b.Gv, &b.r, &b.rp, &b.Gp,
+                         &b.vbest, &b.v1, &b.v0, &b.vin, &b.dotv, &b.xi};
+        for (double **p : d2)
+            if ((rc = grow(p, n2))) return rc;
+        if ((rc = grow(&b.w, (size_t)cap))) return rc;
+        if ((rc = grow(&b.cell, (size_t)cap))) return rc;
+        if ((rc = grow(&b.inv, (size_t)cap))) return rc;
+        if ((rc = grow(&b.perm, (size_t)cap))) return rc;
+        if ((rc = grow(&b.scell, (size_t)cap))) return rc;
+        if ((rc = grow(&b.sw, (size_t)cap))) return rc;
+        if ((rc = grow(&b.sphi, 6 * (size_t)cap))) return rc;
+        if ((rc = grow(&b.px, (size_t)cap))) return rc;
+        if ((rc = grow(&b.pg, (size_t)cap))) return rc;
+        if ((rc = grow(&b.pw, (size_t)cap))) return rc;
+        if ((rc = grow(&b.pf_x, (size_t)cap))) return rc;
+        if ((rc = grow(&b.pf_g, (size_t)cap))) return rc;
+        if ((rc = grow(&b.pf_w, (size_t)cap))) return rc;
+        if ((rc = grow(&b.pdot, n2))) return rc;
+        if ((rc = grow(&b.pA, 3 * (size_t)cap))) return rc;
+        int nchunk = co_cdiv(cap, CO_CHUNK);
+        if ((rc = grow(&b.hist, (size_t)nchunk * c->n_el))) return rc;
+        if ((rc = grow(&b.hoff, (size_t)nchunk * c->n_el))) return rc;
+        b.nchunk_cap = nchunk;
+        b.cap = cap;
+        if (b.m_cap > 0) {
+            if ((rc = grow(&b.dF, n2 * b.m_cap))) return rc;
+            if ((rc = grow(&b.dG, n2 * b.m_cap))) return rc;
+        }
+    }
+    if (m > b.m_cap) {
+        size_t n2 = 2 * (size_t)b.cap;
+        if ((rc = grow(&b.dF, n2 * m))) return rc;
+        if ((rc = grow(&b.dG, n2 * m))) return rc;
+        b.m_cap = m;
+    }
+    return CO_OK;
+}

@@ -1,0 +1,165 @@
+/*
+ * collops.h -- C ABI of the GB300 (sm_103a) collision-operator library.
+ *
+ * Drop-in for the hot-loop hooks of CollisionOperators.jl: each entry point
+ * replaces one Julia routine that solver.jl reaches through COLLISION_FN,
+ * COLLMETRIC_FN, L2PROJ_FN, COMPG_FN or LOGGRAD_FN (solver.jl:30-34), plus the
+ * CPU stages between them (quadrature, mass solve) and the whole implicit step.
+ *
+ * Conventions
+ *  - Marker arrays are the reference's Julia Matrix{Float64} N x 2 in
+ *    column-major order: v[0..N-1] = v1, v[N..2N-1] = v2. G, g, dot_v likewise;
+ *    A is N x 3 (A11, A12, A22 columns). w is a length-N vector.
+ *  - Coefficient vectors (f_coeffs, r, L) have length n_dofs =
+ *    (n_el1 + 2)(n_el2 + 2), index i1 + i2*(n_el1 + 2) (first dimension fastest,
+ *    MantisWrappers.jl:136 and projection_gpu.jl:66, 0-based here).
+ *  - Plain entry points take HOST pointers; the library copies in and out on
+ *    its own stream and returns after the result is on the host. The *_dev
+ *    variants take device pointers and leave results in device memory.
+ *  - Every entry point returns an int status: CO_OK or a CO_ERR_* code. The
+ *    library never falls back to a CPU path.
+ *  - One context per mesh and device; calls on a context must not overlap
+ *    (the reference never calls a hook concurrently).
+ */
+#ifndef COLLOPS_H
+#define COLLOPS_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CO_ABI_VERSION 1
+
+#define CO_OK 0
+#define CO_ERR_ARG 1          /* bad argument (NULL, N < 0, sizes)             */
+#define CO_ERR_CUDA 2         /* a CUDA runtime call failed                    */
+#define CO_ERR_UNSUPPORTED 3  /* e.g. P_DEG != 2 (enable_gpu! keeps the CPU)   */
+#define CO_ERR_NONFINITE 4    /* NaN/Inf in the inputs or in a residual        */
+#define CO_ERR_TIMEOUT 5      /* a bounded device-side wait gave up            */
+#define CO_ERR_NOMEM 6        /* device allocation failed                      */
+#define CO_ERR_NODEVICE 7     /* no CUDA device visible                        */
+
+/* context flags */
+#define CO_FLAG_LOGSQ 1u      /* use_logsq (Parameters.jl:63; functions.jl:9)  */
+#define CO_FLAG_FP32_PAIR 2u  /* gpu_fp32 (Parameters.jl:133): co_collision
+                                 runs the mixed FP32 pair sum                  */
+
+/* model */
+#define CO_MODEL_LANDAU 0
+#define CO_MODEL_LB 1
+
+/* precision of the implicit solve */
+#define CO_PREC_FP64 0        /* plain FP64 form                                */
+#define CO_PREC_MIXED 1       /* FP32 pair maps, FP64 exit Picard map           */
+
+typedef struct co_ctx co_ctx;
+
+/* Solver options: the SimParameters fields step_anderson! reads
+ * (Parameters.jl:50-106, solver.jl:305-312), plus the precision form. */
+typedef struct {
+    int model;               /* CO_MODEL_LANDAU / CO_MODEL_LB (collision_model) */
+    double nu;               /* LB collision frequency                          */
+    int use_gonzalez;
+    int use_anderson;
+    int exit_picard_step;
+    int m;                   /* Anderson depth, 1..8                            */
+    int max_iter;
+    double tol;
+    double abs_floor;
+    int stag_window;
+    double stag_rel_tol;
+    int damp_decay_start;
+    double damp_decay_factor;
+    double restart_factor;   /* <= 0 means Inf                                  */
+    double damping;
+    double reg_factor;
+    int precision;           /* CO_PREC_FP64 or CO_PREC_MIXED                   */
+    double mixed_floor;      /* mixed form: absolute residual floor of the FP32
+                                phase; <= 0 selects the default                 */
+} co_opts;
+
+/* Library version (CO_ABI_VERSION). */
+int co_version(void);
+/* Human-readable status text. */
+const char *co_strerror(int status);
+
+/* Workspace creation: replaces build_workspace (MantisWrappers.jl:90-158) for
+ * the device side -- breakpoints, P_DEG=2 C1 B-spline tables, 1D mass-matrix
+ * inverses, N_QUAD Gauss-Legendre rule. p_deg != 2 -> CO_ERR_UNSUPPORTED (the
+ * reference keeps the CPU projection then, main.jl:396-404). */
+int co_ctx_create(const double *bp1, int nb1, const double *bp2, int nb2,
+                  int p_deg, int n_quad, unsigned flags, int device, co_ctx **out);
+int co_ctx_destroy(co_ctx *ctx);
+/* n_dofs of the context's space. */
+int co_ctx_n_dofs(const co_ctx *ctx, int *n_dofs);
+
+/* COLLISION_FN: compute_collision! (functions.jl:205-237),
+ * compute_collision_gpu! / compute_collision_gpu32! (collision_gpu.jl:233-280). */
+int co_collision(co_ctx *ctx, const double *v, const double *w, const double *G,
+                 double *dot_v, int N);
+
+/* COLLMETRIC_FN: compute_collision_metric! (functions.jl:249-290),
+ * compute_collision_metric_gpu! (collision_gpu.jl:377-402). A is N x 3. */
+int co_collision_metric(co_ctx *ctx, const double *v, const double *w,
+                        const double *G, double *dot_v, double *A, int N);
+
+/* L2PROJ_FN: l2_project! (functions.jl:121-134), l2_project_gpu!
+ * (projection_gpu.jl:213-226); includes the mass solve, deterministic. */
+int co_l2_project(co_ctx *ctx, const double *v, const double *w,
+                  double *f_coeffs, int N);
+
+/* COMPG_FN: compute_G! (functions.jl:182-202), compute_G_gpu!
+ * (projection_gpu.jl:228-246). */
+int co_grad_L(co_ctx *ctx, const double *v, const double *L, double *G, int N);
+
+/* LOGGRAD_FN: eval_loggrad_at_particles! (functions.jl:37-64),
+ * eval_loggrad_gpu! (projection_gpu.jl:251-269). */
+int co_loggrad(co_ctx *ctx, const double *v, const double *f_coeffs, double *g,
+               int N);
+
+/* compute_r! (functions.jl:158-179): CPU-only in the reference. */
+int co_compute_r(co_ctx *ctx, const double *f_coeffs, double *r);
+
+/* compute_entropy (functions.jl:137-155): CPU-only in the reference. */
+int co_entropy(co_ctx *ctx, const double *f_coeffs, double *S);
+
+/* ldiv!(out, ws.M_lu, rhs) (solver.jl:67; projection_gpu.jl:224). */
+int co_mass_solve(co_ctx *ctx, const double *rhs, double *out);
+
+/* picard_map! (solver.jl:176-227), Landau or LB per opts->model. */
+int co_picard_map(co_ctx *ctx, const co_opts *opts, double *v_out,
+                  const double *v_in, const double *v0, const double *w, int N,
+                  double S0, double dt);
+
+/* step_anderson! (solver.jl:300-423) entirely on the device; v1 is the initial
+ * guess in and the solution out. Outputs mirror its return tuple
+ * (iterations, residual, n_restarts, initial residual). */
+int co_step_anderson(co_ctx *ctx, const co_opts *opts, double *v1,
+                     const double *v0, const double *w, int N, double S0,
+                     double dt, int *iters, double *res, int *n_restarts,
+                     double *r0);
+
+/* Same with device pointers (inputs resident in HBM). */
+int co_step_anderson_dev(co_ctx *ctx, const co_opts *opts, double *v1,
+                         const double *v0, const double *w, int N, double S0,
+                         double dt, int *iters, double *res, int *n_restarts,
+                         double *r0);
+
+/* Explicit Euler predictor of the time loop (main.jl:233-245):
+ * v1 = v + dt * vdot(v) with the model's right-hand side. */
+int co_predictor(co_ctx *ctx, const co_opts *opts, double *v1, const double *v,
+                 const double *w, int N, double dt);
+int co_predictor_dev(co_ctx *ctx, const co_opts *opts, double *v1,
+                     const double *v, const double *w, int N, double dt);
+
+/* Entropy of the projection of markers v (f_s(v) -> S), device pointers:
+ * the S0 of the next step (main.jl:228, :298-300). */
+int co_entropy_of_markers_dev(co_ctx *ctx, const double *v, const double *w,
+                              int N, double *S);
+
+/* Number of kernels this context has launched so far. */
+int co_launch_count(const co_ctx *ctx, unsigned long long *launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

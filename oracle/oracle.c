@@ -1,0 +1,836 @@
+/*
+ * oracle.c -- CPU FP64 restatement of the CollisionOperators.jl hot path.
+ * TEST INFRASTRUCTURE ONLY (parity checker and timed CPU baseline); the shipped
+ * library never links or calls it. Parity status: partially pinned -- see
+ * oracle.h for what pins it.
+ *
+ * Each function restates one reference routine in the same loop order and with
+ * the same guards and clamps; citations are file:line in the reference tree.
+ * The Mantis.jl pieces (B-spline space, extraction, Gauss-Legendre rule, mass
+ * matrix) are restated from the mathematics:
+ *   - clamped quadratic knot vector on the breakpoints, single interior knots
+ *     (regularity 1): n_dofs_1d = n_el + 2, element e carries basis e, e+1, e+2;
+ *   - Bezier extraction of that space (knot insertion for quadratics);
+ *   - Gauss-Legendre nodes mapped to [0,1], weights summing to 1, times the
+ *     element area;
+ *   - the mass matrix assembled element by element with the 3x3 rule, then
+ *     factorised (banded Cholesky instead of sparse LU; same solution up to
+ *     round-off).
+ * Compile with -ffp-contract=off: Julia does not fuse a*b+c unless asked to.
+ */
+#include "oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define FS_FLOOR 1e-30 /* functions.jl:23 */
+#define G_MAX 100.0    /* functions.jl:31 */
+
+struct om_mesh {
+    int n1, n2;          /* elements per dimension */
+    double *bp1, *bp2;   /* n+1 breakpoints each */
+    int nd1, nd2, n_dofs, n_el;
+    double *C1, *C2;     /* extraction [n][3][3]: phi_j = sum_k C[k][j] B_k */
+    int nq;
+    double qx[32], qw[32];
+    int bw;              /* half bandwidth of the 2D mass matrix */
+    double *Lb;          /* banded Cholesky factor, row i: cols i-bw..i */
+    int use_logsq;
+};
+
+/* ---------------------------------------------------------------- quadrature */
+
+/* Gauss-Legendre rule on [0,1] (weights sum to 1) by Newton on P_n. */
+static void gauss_legendre01(int n, double *x, double *w) {
+    for (int i = 0; i < n; i++) {
+        double z = cos(M_PI * (i + 0.75) / (n + 0.5));
+        double pp = 0.0;
+        for (int it = 0; it < 100; it++) {
+            double p0 = 1.0, p1 = z;
+            for (int k = 2; k <= n; k++) {
+                double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+                p0 = p1;
+                p1 = p2;
+            }
+            if (n == 1) { p1 = z; p0 = 1.0; }
+            pp = n * (z * p1 - p0) / (z * z - 1.0);
+            double dz = p1 / pp;
+            z -= dz;
+            if (fabs(dz) < 1e-16) break;
+        }
+        {
+            double p0 = 1.0, p1 = z;
+            for (int k = 2; k <= n; k++) {
+                double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+                p0 = p1;
+                p1 = p2;
+            }
+            pp = n * (z * p1 - p0) / (z * z - 1.0);
+        }
+        /* ascending order on [0,1] */
+        x[i] = 0.5 * (1.0 + z);
+        w[i] = 1.0 / ((1.0 - z * z) * pp * pp);
+    }
+    /* sort ascending (cos gives descending z) */
+    for (int i = 0; i < n / 2; i++) {
+        double t = x[i]; x[i] = x[n - 1 - i]; x[n - 1 - i] = t;
+        t = w[i]; w[i] = w[n - 1 - i]; w[n - 1 - i] = t;
+    }
+}
+
+/* ------------------------------------------------------------------- basis */
+
+/* Bezier extraction of the clamped C1 quadratic B-spline space on breakpoints
+ * bp[0..n]: element e with neighbour widths hl (left), h, hr (right), hl = 0 at
+ * the first element and hr = 0 at the last. */
+static void build_extraction(const double *bp, int n, double *C) {
+    for (int e = 0; e < n; e++) {
+        double h = bp[e + 1] - bp[e];
+        double hl = e > 0 ? bp[e] - bp[e - 1] : 0.0;
+        double hr = e < n - 1 ? bp[e + 2] - bp[e + 1] : 0.0;
+        double *c = C + 9 * e; /* c[k*3 + j] */
+        memset(c, 0, 9 * sizeof(double));
+        c[0 * 3 + 0] = h / (hl + h);
+        c[0 * 3 + 1] = hl / (hl + h);
+        c[1 * 3 + 1] = 1.0;
+        c[2 * 3 + 1] = hr / (h + hr);
+        c[2 * 3 + 2] = h / (h + hr);
+    }
+}
+
+/* _bernstein_eval! for p = 2 (MantisWrappers.jl:201-216), same expression
+ * order: binomial(p,i) * xi^i * (1-xi)^(p-i) and p*(left - right). */
+static void bern2(double xi, double *B, double *dB) {
+    double om = 1.0 - xi;
+    B[0] = 1.0 * 1.0 * (om * om);
+    B[1] = 2.0 * xi * om;
+    B[2] = 1.0 * (xi * xi) * 1.0;
+    if (dB) {
+        dB[0] = 2.0 * (0.0 - 1.0 * 1.0 * om);
+        dB[1] = 2.0 * (1.0 * 1.0 * om - 1.0 * xi * 1.0);
+        dB[2] = 2.0 * (1.0 * xi * 1.0 - 0.0);
+    }
+}
+
+/* mul!(phi, transpose(C), B) */
+static void extract3(const double *c, const double *B, double *phi) {
+    for (int j = 0; j < 3; j++)
+        phi[j] = c[0 * 3 + j] * B[0] + c[1 * 3 + j] * B[1] + c[2 * 3 + j] * B[2];
+}
+
+/* searchsortedlast(bp, x) - 1 for bp[0] < x < bp[n] */
+static int search_last(const double *bp, int n, double x) {
+    int lo = 0, hi = n; /* bp[lo] <= x < bp[hi] */
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (bp[mid] <= x) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+typedef struct {
+    int i, j;          /* element indices (0-based) */
+    double xi1, xi2, h1, h2;
+} loc_t;
+
+/* locate_particle (MantisWrappers.jl:168-179) */
+static int locate(const om_mesh *m, double v1, double v2, loc_t *L) {
+    if (v1 <= m->bp1[0] || v1 >= m->bp1[m->n1] || v2 <= m->bp2[0] ||
+        v2 >= m->bp2[m->n2])
+        return 0;
+    int i = search_last(m->bp1, m->n1, v1);
+    int j = search_last(m->bp2, m->n2, v2);
+    L->i = i;
+    L->j = j;
+    L->h1 = m->bp1[i + 1] - m->bp1[i];
+    L->h2 = m->bp2[j + 1] - m->bp2[j];
+    L->xi1 = (v1 - m->bp1[i]) / L->h1;
+    L->xi2 = (v2 - m->bp2[j]) / L->h2;
+    return 1;
+}
+
+/* fast_eval_particle[_grad]! (MantisWrappers.jl:219-289): k = j1 + 3*j2 */
+static void eval_particle(const om_mesh *m, const loc_t *L, double *vals,
+                          double *dx1, double *dx2, int *gids) {
+    double B1[3], dB1[3], B2[3], dB2[3], p1[3], dp1[3], p2[3], dp2[3];
+    bern2(L->xi1, B1, dB1);
+    bern2(L->xi2, B2, dB2);
+    extract3(m->C1 + 9 * L->i, B1, p1);
+    extract3(m->C2 + 9 * L->j, B2, p2);
+    if (dx1) {
+        extract3(m->C1 + 9 * L->i, dB1, dp1);
+        extract3(m->C2 + 9 * L->j, dB2, dp2);
+    }
+    int k = 0;
+    for (int j2 = 0; j2 < 3; j2++)
+        for (int j1 = 0; j1 < 3; j1++) {
+            vals[k] = p1[j1] * p2[j2];
+            if (dx1) {
+                dx1[k] = dp1[j1] * p2[j2];
+                dx2[k] = p1[j1] * dp2[j2];
+            }
+            gids[k] = (L->i + j1) + (L->j + j2) * m->nd1;
+            k++;
+        }
+}
+
+/* ------------------------------------------------------------- mass matrix */
+
+static void assemble_mass_band(om_mesh *m) {
+    int nd = m->n_dofs, bw = m->bw;
+    double *A = calloc((size_t)nd * (bw + 1), sizeof(double)); /* A[i][bw - (i-j)] */
+    double gx[3], gw[3];
+    gauss_legendre01(3, gx, gw);
+    for (int ej = 0; ej < m->n2; ej++)
+        for (int ei = 0; ei < m->n1; ei++) {
+            double h1 = m->bp1[ei + 1] - m->bp1[ei];
+            double h2 = m->bp2[ej + 1] - m->bp2[ej];
+            double jac = h1 * h2;
+            for (int q2 = 0; q2 < 3; q2++)
+                for (int q1 = 0; q1 < 3; q1++) {
+                    double B1[3], B2[3], p1[3], p2[3];
+                    bern2(gx[q1], B1, NULL);
+                    bern2(gx[q2], B2, NULL);
+                    extract3(m->C1 + 9 * ei, B1, p1);
+                    extract3(m->C2 + 9 * ej, B2, p2);
+                    double wq = gw[q1] * gw[q2];
+                    for (int a2 = 0; a2 < 3; a2++)
+                        for (int a1 = 0; a1 < 3; a1++) {
+                            int gi = (ei + a1) + (ej + a2) * m->nd1;
+                            double fi = p1[a1] * p2[a2];
+                            for (int b2 = 0; b2 < 3; b2++)
+                                for (int b1 = 0; b1 < 3; b1++) {
+                                    int gj = (ei + b1) + (ej + b2) * m->nd1;
+                                    if (gj > gi) continue;
+                                    double fj = p1[b1] * p2[b2];
+                                    A[(size_t)gi * (bw + 1) + (bw - (gi - gj))] +=
+                                        fi * fj * wq * jac;
+                                }
+                        }
+                }
+        }
+    /* banded Cholesky, in place */
+    for (int i = 0; i < nd; i++) {
+        int j0 = i - bw < 0 ? 0 : i - bw;
+        for (int j = j0; j <= i; j++) {
+            double s = A[(size_t)i * (bw + 1) + (bw - (i - j))];
+            int k0 = (i - bw > j - bw ? i - bw : j - bw);
+            if (k0 < 0) k0 = 0;
+            for (int k = k0; k < j; k++)
+                s -= A[(size_t)i * (bw + 1) + (bw - (i - k))] *
+                     A[(size_t)j * (bw + 1) + (bw - (j - k))];
+            if (j == i)
+                A[(size_t)i * (bw + 1) + bw] = sqrt(s);
+            else
+                A[(size_t)i * (bw + 1) + (bw - (i - j))] =
+                    s / A[(size_t)j * (bw + 1) + bw];
+        }
+    }
+    m->Lb = A;
+}
+
+void om_mass_solve(const om_mesh *m, const double *rhs, double *out) {
+    int nd = m->n_dofs, bw = m->bw;
+    const double *A = m->Lb;
+    double *y = malloc(sizeof(double) * nd);
+    for (int i = 0; i < nd; i++) {
+        double s = rhs[i];
+        int k0 = i - bw < 0 ? 0 : i - bw;
+        for (int k = k0; k < i; k++) s -= A[(size_t)i * (bw + 1) + (bw - (i - k))] * y[k];
+        y[i] = s / A[(size_t)i * (bw + 1) + bw];
+    }
+    for (int i = nd - 1; i >= 0; i--) {
+        double s = y[i];
+        int k1 = i + bw >= nd ? nd - 1 : i + bw;
+        for (int k = i + 1; k <= k1; k++) s -= A[(size_t)k * (bw + 1) + (bw - (k - i))] * out[k];
+        out[i] = s / A[(size_t)i * (bw + 1) + bw];
+    }
+    free(y);
+}
+
+void om_mass_matrix_dense(const om_mesh *m, double *out) {
+    int nd = m->n_dofs, bw = m->bw;
+    /* rebuild L L^T from the factor */
+    memset(out, 0, sizeof(double) * (size_t)nd * nd);
+    for (int i = 0; i < nd; i++)
+        for (int j = (i - bw < 0 ? 0 : i - bw); j <= i; j++) {
+            double s = 0.0;
+            int k0 = i - bw > j - bw ? i - bw : j - bw;
+            if (k0 < 0) k0 = 0;
+            for (int k = k0; k <= j; k++)
+                s += m->Lb[(size_t)i * (bw + 1) + (bw - (i - k))] *
+                     m->Lb[(size_t)j * (bw + 1) + (bw - (j - k))];
+            out[(size_t)i * nd + j] = s;
+            out[(size_t)j * nd + i] = s;
+        }
+}
+
+/* -------------------------------------------------------------- workspace */
+
+om_mesh *om_create(const double *bp1, int nb1, const double *bp2, int nb2,
+                   int nquad, int use_logsq) {
+    if (nb1 < 2 || nb2 < 2 || nquad < 1 || nquad > 32) return NULL;
+    om_mesh *m = calloc(1, sizeof(om_mesh));
+    m->n1 = nb1 - 1;
+    m->n2 = nb2 - 1;
+    m->bp1 = malloc(sizeof(double) * nb1);
+    m->bp2 = malloc(sizeof(double) * nb2);
+    memcpy(m->bp1, bp1, sizeof(double) * nb1);
+    memcpy(m->bp2, bp2, sizeof(double) * nb2);
+    m->nd1 = m->n1 + 2;
+    m->nd2 = m->n2 + 2;
+    m->n_dofs = m->nd1 * m->nd2;
+    m->n_el = m->n1 * m->n2;
+    m->C1 = malloc(sizeof(double) * 9 * m->n1);
+    m->C2 = malloc(sizeof(double) * 9 * m->n2);
+    build_extraction(m->bp1, m->n1, m->C1);
+    build_extraction(m->bp2, m->n2, m->C2);
+    m->nq = nquad;
+    gauss_legendre01(nquad, m->qx, m->qw);
+    m->bw = 2 * m->nd1 + 2;
+    m->use_logsq = use_logsq;
+    assemble_mass_band(m);
+    return m;
+}
+
+void om_destroy(om_mesh *m) {
+    if (!m) return;
+    free(m->bp1); free(m->bp2); free(m->C1); free(m->C2); free(m->Lb);
+    free(m);
+}
+
+int om_n_dofs(const om_mesh *m) { return m->n_dofs; }
+int om_nd1(const om_mesh *m) { return m->nd1; }
+
+void om_extraction(const om_mesh *m, int dim, double *out) {
+    if (dim == 1) memcpy(out, m->C1, sizeof(double) * 9 * m->n1);
+    else memcpy(out, m->C2, sizeof(double) * 9 * m->n2);
+}
+
+void om_quadrature(const om_mesh *m, double *x, double *w) {
+    memcpy(x, m->qx, sizeof(double) * m->nq);
+    memcpy(w, m->qw, sizeof(double) * m->nq);
+}
+
+/* -------------------------------------------------------------- projection */
+
+void om_l2_rhs(const om_mesh *m, const double *v, const double *w, int N,
+               double *rhs) {
+    memset(rhs, 0, sizeof(double) * m->n_dofs);
+    for (int a = 0; a < N; a++) {
+        loc_t L;
+        if (!locate(m, v[a], v[N + a], &L)) continue;
+        double vals[9];
+        int gids[9];
+        eval_particle(m, &L, vals, NULL, NULL, gids);
+        for (int j = 0; j < 9; j++) rhs[gids[j]] += w[a] * vals[j];
+    }
+}
+
+/* l2_project! (functions.jl:121-134) */
+void om_l2_project(const om_mesh *m, const double *v, const double *w, int N,
+                   double *f_out) {
+    double *rhs = malloc(sizeof(double) * m->n_dofs);
+    om_l2_rhs(m, v, w, N, rhs);
+    om_mass_solve(m, rhs, f_out);
+    free(rhs);
+}
+
+/* field value and basis at quadrature point (q1, q2) of element (ei, ej) */
+static double field_at_qp(const om_mesh *m, const double *c, int ei, int ej,
+                          int q1, int q2, double *phi, int *gids) {
+    double B1[3], B2[3], p1[3], p2[3];
+    bern2(m->qx[q1], B1, NULL);
+    bern2(m->qx[q2], B2, NULL);
+    extract3(m->C1 + 9 * ei, B1, p1);
+    extract3(m->C2 + 9 * ej, B2, p2);
+    double f = 0.0;
+    int k = 0;
+    for (int j2 = 0; j2 < 3; j2++)
+        for (int j1 = 0; j1 < 3; j1++) {
+            phi[k] = p1[j1] * p2[j2];
+            gids[k] = (ei + j1) + (ej + j2) * m->nd1;
+            f += c[gids[k]] * phi[k];
+            k++;
+        }
+    return f;
+}
+
+/* compute_entropy (functions.jl:137-155) */
+double om_entropy(const om_mesh *m, const double *f) {
+    double S = 0.0;
+    for (int ej = 0; ej < m->n2; ej++)
+        for (int ei = 0; ei < m->n1; ei++) {
+            double jac = (m->bp1[ei + 1] - m->bp1[ei]) * (m->bp2[ej + 1] - m->bp2[ej]);
+            for (int q2 = 0; q2 < m->nq; q2++)
+                for (int q1 = 0; q1 < m->nq; q1++) {
+                    double phi[9];
+                    int gids[9];
+                    double fv = field_at_qp(m, f, ei, ej, q1, q2, phi, gids);
+                    double wq = m->qw[q1] * m->qw[q2];
+                    if (m->use_logsq) {
+                        if (fv * fv > 1e-60)
+                            S -= fv * 0.5 * log(fv * fv) * wq * jac;
+                    } else if (fv > 1e-30) {
+                        S -= fv * log(fv) * wq * jac;
+                    }
+                }
+        }
+    return S;
+}
+
+/* compute_r! (functions.jl:158-179) */
+void om_compute_r(const om_mesh *m, const double *f, double *r) {
+    memset(r, 0, sizeof(double) * m->n_dofs);
+    for (int ej = 0; ej < m->n2; ej++)
+        for (int ei = 0; ei < m->n1; ei++) {
+            double jac = (m->bp1[ei + 1] - m->bp1[ei]) * (m->bp2[ej + 1] - m->bp2[ej]);
+            for (int q2 = 0; q2 < m->nq; q2++)
+                for (int q1 = 0; q1 < m->nq; q1++) {
+                    double phi[9];
+                    int gids[9];
+                    double fv = field_at_qp(m, f, ei, ej, q1, q2, phi, gids);
+                    double integrand;
+                    if (m->use_logsq)
+                        integrand = fv * fv > 1e-60 ? (1 + 0.5 * log(fv * fv)) : 0.0;
+                    else
+                        integrand = fv > 1e-30 ? (1 + log(fv)) : 0.0;
+                    double wq = m->qw[q1] * m->qw[q2];
+                    for (int j = 0; j < 9; j++)
+                        r[gids[j]] += integrand * phi[j] * wq * jac;
+                }
+        }
+}
+
+/* compute_G! (functions.jl:182-202) */
+void om_compute_G(const om_mesh *m, const double *v, int N, const double *Lv,
+                  double *G) {
+    for (int a = 0; a < N; a++) {
+        G[a] = 0.0;
+        G[N + a] = 0.0;
+        loc_t L;
+        if (!locate(m, v[a], v[N + a], &L)) continue;
+        double vals[9], dx1[9], dx2[9];
+        int gids[9];
+        eval_particle(m, &L, vals, dx1, dx2, gids);
+        double ih1 = 1.0 / L.h1, ih2 = 1.0 / L.h2;
+        double acc1 = 0.0, acc2 = 0.0;
+        for (int j = 0; j < 9; j++) {
+            double c = Lv[gids[j]];
+            acc1 += c * dx1[j] * ih1;
+            acc2 += c * dx2[j] * ih2;
+        }
+        G[a] = acc1;
+        G[N + a] = acc2;
+    }
+}
+
+/* eval_loggrad_at_particles! (functions.jl:37-64) */
+void om_loggrad(const om_mesh *m, const double *v, int N, const double *fc,
+                double *g) {
+    for (int a = 0; a < N; a++) {
+        loc_t L;
+        if (!locate(m, v[a], v[N + a], &L)) {
+            g[a] = 0.0;
+            g[N + a] = 0.0;
+            continue;
+        }
+        double vals[9], dx1[9], dx2[9];
+        int gids[9];
+        eval_particle(m, &L, vals, dx1, dx2, gids);
+        double ih1 = 1.0 / L.h1, ih2 = 1.0 / L.h2;
+        double f = 0.0, d1 = 0.0, d2 = 0.0;
+        for (int j = 0; j < 9; j++) {
+            double c = fc[gids[j]];
+            f += c * vals[j];
+            d1 += c * dx1[j] * ih1;
+            d2 += c * dx2[j] * ih2;
+        }
+        double invf = 1.0 / fmax(fabs(f), FS_FLOOR);
+        double g1 = d1 * invf, g2 = d2 * invf;
+        g[a] = g1 < -G_MAX ? -G_MAX : (g1 > G_MAX ? G_MAX : g1);
+        g[N + a] = g2 < -G_MAX ? -G_MAX : (g2 > G_MAX ? G_MAX : g2);
+    }
+}
+
+double om_eval_field(const om_mesh *m, const double *c, double x1, double x2) {
+    loc_t L;
+    if (!locate(m, x1, x2, &L)) return 0.0;
+    double vals[9];
+    int gids[9];
+    eval_particle(m, &L, vals, NULL, NULL, gids);
+    double f = 0.0;
+    for (int j = 0; j < 9; j++) f += c[gids[j]] * vals[j];
+    return f;
+}
+
+/* --------------------------------------------------------------- pair sums */
+
+static int set_threads(int nthreads) {
+#ifdef _OPENMP
+    return nthreads > 0 ? nthreads : omp_get_max_threads();
+#else
+    (void)nthreads;
+    return 1;
+#endif
+}
+
+static inline int outside(const om_mesh *m, double a, double b) {
+    return a <= m->bp1[0] || a >= m->bp1[m->n1] || b <= m->bp2[0] || b >= m->bp2[m->n2];
+}
+
+/* one target row of compute_collision! (functions.jl:211-234) */
+static void collision_row(const om_mesh *m, const double *v, const double *w,
+                          const double *G, int N, int g, double *o1, double *o2) {
+    double vg1 = v[g], vg2 = v[N + g];
+    *o1 = 0.0;
+    *o2 = 0.0;
+    if (outside(m, vg1, vg2)) return;
+    double Gg1 = G[g], Gg2 = G[N + g];
+    double acc1 = 0.0, acc2 = 0.0;
+    for (int a = 0; a < N; a++) {
+        if (a == g) continue;
+        double va1 = v[a], va2 = v[N + a];
+        if (outside(m, va1, va2)) continue;
+        double d1 = vg1 - va1;
+        double d2 = vg2 - va2;
+        double dist2 = d1 * d1 + d2 * d2;
+        if (dist2 < 1e-24) continue;
+        double dist = sqrt(dist2);
+        double g1 = G[a] - Gg1;
+        double g2 = G[N + a] - Gg2;
+        double dvg = (d1 * g1 + d2 * g2) / dist2;
+        double inv = 1.0 / dist;
+        acc1 += w[a] * (g1 - d1 * dvg) * inv;
+        acc2 += w[a] * (g2 - d2 * dvg) * inv;
+    }
+    *o1 = acc1;
+    *o2 = acc2;
+}
+
+/* compute_collision! (functions.jl:205-237): threaded over gamma as
+ * Threads.@threads does at functions.jl:210 */
+void om_collision(const om_mesh *m, const double *v, const double *w,
+                  const double *G, int N, double *dot_v, int nthreads) {
+    int nt = set_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nt)
+    for (int g = 0; g < N; g++) collision_row(m, v, w, G, N, g, &dot_v[g], &dot_v[N + g]);
+}
+
+void om_collision_rows(const om_mesh *m, const double *v, const double *w,
+                       const double *G, int N, const int *rows, int nrows,
+                       double *out, int nthreads) {
+    int nt = set_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nt)
+    for (int r = 0; r < nrows; r++)
+        collision_row(m, v, w, G, N, rows[r], &out[r], &out[nrows + r]);
+}
+
+/* compute_collision_metric! (functions.jl:249-290) */
+void om_collision_metric(const om_mesh *m, const double *v, const double *w,
+                         const double *G, int N, double *dot_v, double *A,
+                         int nthreads) {
+    int nt = set_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nt)
+    for (int g = 0; g < N; g++) {
+        double vg1 = v[g], vg2 = v[N + g];
+        dot_v[g] = dot_v[N + g] = 0.0;
+        A[g] = A[N + g] = A[2 * N + g] = 0.0;
+        if (outside(m, vg1, vg2)) continue;
+        double Gg1 = G[g], Gg2 = G[N + g];
+        double acc1 = 0.0, acc2 = 0.0, a11 = 0.0, a12 = 0.0, a22 = 0.0;
+        for (int a = 0; a < N; a++) {
+            if (a == g) continue;
+            double va1 = v[a], va2 = v[N + a];
+            if (outside(m, va1, va2)) continue;
+            double d1 = vg1 - va1;
+            double d2 = vg2 - va2;
+            double dist2 = d1 * d1 + d2 * d2;
+            if (dist2 < 1e-24) continue;
+            double dist = sqrt(dist2);
+            double g1 = G[a] - Gg1;
+            double g2 = G[N + a] - Gg2;
+            double dvg = (d1 * g1 + d2 * g2) / dist2;
+            double inv = 1.0 / dist;
+            acc1 += w[a] * (g1 - d1 * dvg) * inv;
+            acc2 += w[a] * (g2 - d2 * dvg) * inv;
+            double s = w[a] * inv;
+            a11 += s * (1 - d1 * d1 / dist2);
+            a12 -= s * d1 * d2 / dist2;
+            a22 += s * (1 - d2 * d2 / dist2);
+        }
+        dot_v[g] = acc1;
+        dot_v[N + g] = acc2;
+        A[g] = a11;
+        A[N + g] = a12;
+        A[2 * N + g] = a22;
+    }
+}
+
+/* ---------------------------------------------------------------------- LB */
+
+void om_moments(const double *v, const double *w, int N, double *out) {
+    double n = 0.0, U1 = 0.0, U2 = 0.0, Q = 0.0;
+    for (int a = 0; a < N; a++) {
+        double wa = w[a], x = v[a], y = v[N + a];
+        n += wa;
+        U1 += wa * x;
+        U2 += wa * y;
+        Q += wa * (x * x + y * y);
+    }
+    out[0] = n; out[1] = U1; out[2] = U2; out[3] = Q;
+}
+
+/* dense LU with partial pivoting, as Julia's `\` (LAPACK getrf/getrs) */
+static int lu_solve(int n, double *A, double *b) {
+    int piv[32];
+    for (int k = 0; k < n; k++) {
+        int p = k;
+        double mx = fabs(A[k * n + k]);
+        for (int i = k + 1; i < n; i++)
+            if (fabs(A[i * n + k]) > mx) { mx = fabs(A[i * n + k]); p = i; }
+        piv[k] = p;
+        if (p != k)
+            for (int j = 0; j < n; j++) { double t = A[k * n + j]; A[k * n + j] = A[p * n + j]; A[p * n + j] = t; }
+        if (A[k * n + k] == 0.0) return 1;
+        for (int i = k + 1; i < n; i++) {
+            A[i * n + k] /= A[k * n + k];
+            for (int j = k + 1; j < n; j++) A[i * n + j] -= A[i * n + k] * A[k * n + j];
+        }
+    }
+    for (int k = 0; k < n; k++) if (piv[k] != k) { double t = b[k]; b[k] = b[piv[k]]; b[piv[k]] = t; }
+    for (int i = 0; i < n; i++) for (int j = 0; j < i; j++) b[i] -= A[i * n + j] * b[j];
+    for (int i = n - 1; i >= 0; i--) {
+        for (int j = i + 1; j < n; j++) b[i] -= A[i * n + j] * b[j];
+        b[i] /= A[i * n + i];
+    }
+    return 0;
+}
+
+void om_drift_multipliers(const double *v, const double *w, const double *g,
+                          int N, double n, double U1, double U2, double Q,
+                          double *out) {
+    double Sg1 = 0.0, Sg2 = 0.0, P = 0.0;
+    for (int a = 0; a < N; a++) {
+        double g1 = g[a], g2 = g[N + a], wa = w[a];
+        Sg1 += wa * g1;
+        Sg2 += wa * g2;
+        P += wa * (v[a] * g1 + v[N + a] * g2);
+    }
+    double M[9] = {n, 0.0, U1, 0.0, n, U2, U1, U2, Q};
+    double rhs[3] = {-Sg1, -Sg2, -P};
+    lu_solve(3, M, rhs);
+    out[0] = rhs[0]; out[1] = rhs[1]; out[2] = rhs[2];
+}
+
+void om_lb_velocity(double *dot_v, const double *v, const double *g, int N,
+                    double A1, double A2, double B, double nu) {
+    for (int a = 0; a < N; a++) {
+        dot_v[a] = -nu * (g[a] + A1 + B * v[a]);
+        dot_v[N + a] = -nu * (g[N + a] + A2 + B * v[N + a]);
+    }
+}
+
+/* ------------------------------------------------------------ Picard map */
+
+/* compute_entropy_gradient! (solver.jl:62-74) */
+static void entropy_gradient(const om_mesh *m, double *dS, const double *v,
+                             const double *w, int N, double *fbuf, double *r,
+                             double *L, double *G) {
+    om_l2_project(m, v, w, N, fbuf);
+    om_compute_r(m, fbuf, r);
+    om_mass_solve(m, r, L);
+    om_compute_G(m, v, N, L, G);
+    for (int a = 0; a < N; a++) {
+        dS[a] = -w[a] * G[a];
+        dS[N + a] = -w[a] * G[N + a];
+    }
+}
+
+/* picard_map! (solver.jl:176-227), with landau_geff! (solver.jl:86-113) */
+void om_picard_map(const om_mesh *m, const om_opts *o, double *v_out,
+                   const double *v_in, const double *v0, const double *w,
+                   int N, double S0, double dt) {
+    int nd = m->n_dofs;
+    double *v_mid = malloc(sizeof(double) * 2 * N);
+    double *dv = malloc(sizeof(double) * 2 * N);
+    double *dS = malloc(sizeof(double) * 2 * N);
+    double *Geff = malloc(sizeof(double) * 2 * N);
+    double *dotv = malloc(sizeof(double) * 2 * N);
+    double *Gb = malloc(sizeof(double) * 2 * N);
+    double *fbuf = malloc(sizeof(double) * nd);
+    double *r = malloc(sizeof(double) * nd);
+    double *L = malloc(sizeof(double) * nd);
+    for (int i = 0; i < 2 * N; i++) {
+        v_mid[i] = 0.5 * (v0[i] + v_in[i]);
+        dv[i] = v_in[i] - v0[i];
+    }
+    if (o->model == 1) {
+        /* LB: direct clamped log-gradient base (solver.jl:185-210) */
+        om_l2_project(m, v_mid, w, N, fbuf);
+        om_loggrad(m, v_mid, N, fbuf, Geff);
+        if (o->use_gonzalez) {
+            om_l2_project(m, v_in, w, N, fbuf);
+            double S1 = om_entropy(m, fbuf);
+            double dot = 0.0, nrm2 = 0.0;
+            for (int a = 0; a < N; a++) {
+                dot -= w[a] * (dv[a] * Geff[a] + dv[N + a] * Geff[N + a]);
+                nrm2 += dv[a] * dv[a] + dv[N + a] * dv[N + a];
+            }
+            double lam = nrm2 > 1e-30 ? (S1 - S0 - dot) / nrm2 : 0.0;
+            for (int a = 0; a < N; a++) {
+                double iw = 1.0 / w[a];
+                Geff[a] -= lam * dv[a] * iw;
+                Geff[N + a] -= lam * dv[N + a] * iw;
+            }
+        }
+        double mo[4], ab[3];
+        om_moments(v_mid, w, N, mo);
+        om_drift_multipliers(v_mid, w, Geff, N, mo[0], mo[1], mo[2], mo[3], ab);
+        om_lb_velocity(dotv, v_mid, Geff, N, ab[0], ab[1], ab[2], o->nu);
+    } else {
+        entropy_gradient(m, dS, v_mid, w, N, fbuf, r, L, Gb);
+        double corr = 0.0;
+        if (o->use_gonzalez) {
+            om_l2_project(m, v_in, w, N, fbuf);
+            double S1 = om_entropy(m, fbuf);
+            double dot = 0.0, nrm2 = 0.0;
+            for (int a = 0; a < N; a++) {
+                dot += dv[a] * dS[a] + dv[N + a] * dS[N + a];
+                nrm2 += dv[a] * dv[a] + dv[N + a] * dv[N + a];
+            }
+            corr = nrm2 > 1e-30 ? (S1 - S0 - dot) / nrm2 : 0.0;
+        }
+        for (int a = 0; a < N; a++) {
+            double iw = 1.0 / w[a];
+            Geff[a] = -(dS[a] + corr * dv[a]) * iw;
+            Geff[N + a] = -(dS[N + a] + corr * dv[N + a]) * iw;
+        }
+        om_collision(m, v_mid, w, Geff, N, dotv, o->nthreads);
+    }
+    for (int i = 0; i < 2 * N; i++) v_out[i] = v0[i] + dt * dotv[i];
+    free(v_mid); free(dv); free(dS); free(Geff); free(dotv); free(Gb);
+    free(fbuf); free(r); free(L);
+}
+
+static double norm2v(const double *x, int n) {
+    double s = 0.0;
+    for (int i = 0; i < n; i++) s += x[i] * x[i];
+    return sqrt(s);
+}
+
+/* step_anderson! (solver.jl:300-423) */
+void om_step_anderson(const om_mesh *m, const om_opts *o, double *v1,
+                      const double *v0, const double *w, int N, double S0,
+                      double dt, double *out4) {
+    int n = 2 * N, mm = o->m;
+    double *Gv = malloc(sizeof(double) * n), *r = malloc(sizeof(double) * n);
+    double *rp = malloc(sizeof(double) * n), *Gp = malloc(sizeof(double) * n);
+    double *vold = malloc(sizeof(double) * n), *vbest = malloc(sizeof(double) * n);
+    double *dF = calloc((size_t)n * mm, sizeof(double));
+    double *dG = calloc((size_t)n * mm, sizeof(double));
+    double restart = o->restart_factor > 0 ? o->restart_factor : INFINITY;
+    int history = 0, slot = 0, n_restart = 0;
+    double nrm_r0 = 0.0, nrm_r = 0.0, nrm_best = INFINITY, nrm_best_window = INFINITY;
+    memcpy(vbest, v1, sizeof(double) * n);
+    for (int k = 1; k <= o->max_iter; k++) {
+        memcpy(vold, v1, sizeof(double) * n);
+        om_picard_map(m, o, Gv, v1, v0, w, N, S0, dt);
+        for (int i = 0; i < n; i++) r[i] = Gv[i] - v1[i];
+        nrm_r = norm2v(r, n);
+        if (k == 1) nrm_r0 = nrm_r;
+        if (nrm_r < nrm_best) {
+            nrm_best = nrm_r;
+            memcpy(vbest, o->exit_picard_step ? Gv : v1, sizeof(double) * n);
+        }
+        double eff_tol = fmax(o->tol * (norm2v(v1, n) + 1e-30), o->abs_floor);
+        if (nrm_r < eff_tol) {
+            if (o->exit_picard_step) memcpy(v1, Gv, sizeof(double) * n);
+            out4[0] = k; out4[1] = nrm_r; out4[2] = n_restart; out4[3] = nrm_r0;
+            goto done;
+        }
+        if (k > o->stag_window && k % o->stag_window == 0) {
+            double rel = (nrm_best_window - nrm_best) / (nrm_best_window + 1e-30);
+            if (rel < o->stag_rel_tol) {
+                memcpy(v1, vbest, sizeof(double) * n);
+                out4[0] = k; out4[1] = nrm_best; out4[2] = n_restart; out4[3] = nrm_r0;
+                goto done;
+            }
+            nrm_best_window = nrm_best;
+        }
+        int just_restarted = 0;
+        if (k > 1 && nrm_r > restart * nrm_best) {
+            history = 0;
+            slot = 0;
+            n_restart++;
+            just_restarted = 1;
+        }
+        double damp = k > o->damp_decay_start ? o->damping * o->damp_decay_factor : o->damping;
+        if (k == 1 || just_restarted || !o->use_anderson) {
+            for (int i = 0; i < n; i++) v1[i] = damp * Gv[i] + (1 - damp) * vold[i];
+        } else {
+            slot = slot % mm + 1; /* mod1(slot + 1, m) */
+            history = history + 1 < mm ? history + 1 : mm;
+            double *F = dF + (size_t)(slot - 1) * n, *Gc = dG + (size_t)(slot - 1) * n;
+            for (int i = 0; i < n; i++) { F[i] = r[i] - rp[i]; Gc[i] = Gv[i] - Gp[i]; }
+            double ATA[64], ATr[8];
+            for (int a = 0; a < history; a++) {
+                for (int b = 0; b < history; b++) {
+                    double s = 0.0;
+                    const double *Fa = dF + (size_t)a * n, *Fb = dF + (size_t)b * n;
+                    for (int i = 0; i < n; i++) s += Fa[i] * Fb[i];
+                    ATA[a * history + b] = s;
+                }
+                double s = 0.0;
+                const double *Fa = dF + (size_t)a * n;
+                for (int i = 0; i < n; i++) s += Fa[i] * r[i];
+                ATr[a] = s;
+            }
+            double dm = 0.0;
+            for (int j = 0; j < history; j++) dm += ATA[j * history + j];
+            dm /= history;
+            double l2 = o->reg_factor * dm + 1e-30;
+            for (int j = 0; j < history; j++) ATA[j * history + j] += l2;
+            lu_solve(history, ATA, ATr);
+            for (int i = 0; i < n; i++) {
+                double s = Gv[i];
+                for (int j = 0; j < history; j++) s += -1.0 * dG[(size_t)j * n + i] * ATr[j];
+                v1[i] = damp * s + (1 - damp) * vold[i];
+            }
+        }
+        memcpy(rp, r, sizeof(double) * n);
+        memcpy(Gp, Gv, sizeof(double) * n);
+    }
+    memcpy(v1, vbest, sizeof(double) * n);
+    out4[0] = o->max_iter; out4[1] = nrm_best; out4[2] = n_restart; out4[3] = nrm_r0;
+done:
+    free(Gv); free(r); free(rp); free(Gp); free(vold); free(vbest); free(dF); free(dG);
+}
+
+/* Explicit predictor of the time loop (main.jl:233-245). */
+void om_predictor(const om_mesh *m, const om_opts *o, double *v1,
+                  const double *v, const double *w, int N, double dt) {
+    int nd = m->n_dofs;
+    double *fc = malloc(sizeof(double) * nd), *r = malloc(sizeof(double) * nd);
+    double *L = malloc(sizeof(double) * nd);
+    double *G = malloc(sizeof(double) * 2 * N), *dotv = malloc(sizeof(double) * 2 * N);
+    om_l2_project(m, v, w, N, fc);
+    if (o->model == 1) {
+        double mo[4], ab[3];
+        om_loggrad(m, v, N, fc, G);
+        om_moments(v, w, N, mo);
+        om_drift_multipliers(v, w, G, N, mo[0], mo[1], mo[2], mo[3], ab);
+        om_lb_velocity(dotv, v, G, N, ab[0], ab[1], ab[2], o->nu);
+    } else {
+        om_compute_r(m, fc, r);
+        om_mass_solve(m, r, L);
+        om_compute_G(m, v, N, L, G);
+        om_collision(m, v, w, G, N, dotv, o->nthreads);
+    }
+    for (int i = 0; i < 2 * N; i++) v1[i] = v[i] + dt * dotv[i];
+    free(fc); free(r); free(L); free(G); free(dotv);
+}

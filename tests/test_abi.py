@@ -1,0 +1,109 @@
+"""CPU tests of the C-ABI boundary and the host-side mirror (no GPU needed).
+
+- the library builds for sm_103a, loads, and exports every entry point that
+  include/collops.h declares (no compute calls);
+- status codes come back as statuses (no device: CO_ERR_NODEVICE; bad
+  arguments: CO_ERR_ARG; P_DEG != 2: CO_ERR_UNSUPPORTED) rather than crashes;
+- parse_overrides behaves like the reference's (main_helpers.jl:63-72).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, cuda_available
+
+HEADER = os.path.join(ROOT, "include", "collops.h")
+
+
+def declared_symbols():
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(co_[A-Za-z0-9_]+)\s*\(", txt)))
+
+
+def test_header_declares_hooks():
+    syms = declared_symbols()
+    for s in ("co_ctx_create", "co_collision", "co_collision_metric", "co_l2_project",
+              "co_grad_L", "co_loggrad", "co_step_anderson", "co_picard_map"):
+        assert s in syms
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    lib = C.CDLL(built_lib)
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_python_mirror_binds_every_symbol(built_lib, collops_mod):
+    lib = collops_mod.load_library()
+    assert lib.co_version() == 1
+    for s in declared_symbols():
+        assert s in collops_mod._SIGNATURES, f"{s} not bound in collops"
+
+
+def test_strerror_and_status_codes(built_lib, collops_mod):
+    lib = collops_mod.load_library()
+    assert lib.co_strerror(0) == b"ok"
+    assert b"P_DEG" in lib.co_strerror(3)
+    h = C.c_void_p()
+    bp = np.linspace(-6, 6, 17)
+    dp = bp.ctypes.data_as(C.POINTER(C.c_double))
+    # invalid arguments are rejected before any device work
+    assert lib.co_ctx_create(dp, 1, dp, 17, 2, 6, 0, 0, C.byref(h)) == 1
+    assert lib.co_ctx_create(dp, 17, dp, 17, 2, 0, 0, 0, C.byref(h)) == 1
+    assert lib.co_ctx_create(dp, 17, dp, 17, 3, 6, 0, 0, C.byref(h)) == 3
+    bad = np.array([0.0, 1.0, 1.0, 2.0])  # non-increasing breakpoints
+    bdp = bad.ctypes.data_as(C.POINTER(C.c_double))
+    assert lib.co_ctx_create(bdp, 4, dp, 17, 2, 6, 0, 0, C.byref(h)) == 1
+    assert lib.co_collision(None, None, None, None, None, 0) == 1
+    if not cuda_available():
+        assert lib.co_ctx_create(dp, 17, dp, 17, 2, 6, 0, 0, C.byref(h)) == 7
+
+
+def test_opts_struct_layout(collops_mod):
+    # co_opts: 18 fields, natural alignment (x86-64 and aarch64 LP64): 128 bytes
+    assert C.sizeof(collops_mod.CoOpts) == 128
+    o = collops_mod.SimParameters().opts()
+    assert o.m == 8 and o.tol == 1e-12 and o.model == 0
+
+
+def test_parse_overrides(collops_mod):
+    """main_helpers.jl:63-72 restated on the Python mirror."""
+    base = collops_mod.SimParameters(suffix="base")
+    p = collops_mod.parse_overrides(base, ["--suffix=run2", "--DT=0.004", "--N_STEPS=300"])
+    assert p.suffix == "run2" and p.DT == 0.004 and p.N_STEPS == 300
+    assert p.N_PARTICLES == base.N_PARTICLES
+    assert collops_mod.parse_overrides(base, []) is base
+    with pytest.raises(ValueError):
+        collops_mod.parse_overrides(base, ["--no_such_field=1"])
+    with pytest.raises(ValueError):
+        collops_mod.parse_overrides(base, ["--bp1=1"])
+    q = collops_mod.parse_overrides(base, ["--use_gonzalez=0", "--gpu_fp32=true",
+                                           "--collision_model=lb"])
+    assert q.use_gonzalez is False and q.gpu_fp32 is True and q.collision_model == "lb"
+
+
+def test_enable_gpu_hook_selection(collops_mod):
+    """enable_gpu! (main.jl:390-423): which hooks are repointed."""
+    h = collops_mod.enable_gpu(collops_mod.SimParameters())
+    assert h.COLLISION_FN is collops_mod.compute_collision_gpu
+    assert h.COLLMETRIC_FN is collops_mod.compute_collision_metric_gpu
+    assert h.L2PROJ_FN is collops_mod.l2_project_gpu and h.COMPG_FN is collops_mod.compute_G_gpu
+    h = collops_mod.enable_gpu(collops_mod.SimParameters(gpu_fp32=True))
+    assert h.COLLISION_FN is collops_mod.compute_collision_gpu32 and h.COLLMETRIC_FN is None
+    h = collops_mod.enable_gpu(collops_mod.SimParameters(collision_model="lb"))
+    assert h.LOGGRAD_FN is collops_mod.eval_loggrad_gpu and h.COLLISION_FN is None
+    with pytest.raises(collops_mod.CollopsError):
+        collops_mod.enable_gpu(collops_mod.SimParameters(P_DEG=3))
+
+
+def test_output_layout_checked(collops_mod):
+    """Outputs must be column-major float64 (Julia layout); checked before any call."""
+    with pytest.raises(ValueError):
+        collops_mod._out(np.zeros((4, 2)), (4, 2), "dot_v")   # C order
+    collops_mod._out(np.zeros((4, 2), order="F"), (4, 2), "dot_v")
