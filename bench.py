@@ -1,0 +1,544 @@
+#!/usr/bin/env python3
+"""Benchmark: ms per converged implicit step, Landau N = 131,072.
+
+Workload (the precision-form configuration): Landau, N = 131,072 markers from an
+anisotropic Gaussian (T_x = 1.0, T_y = 0.25, i.e. sigma = (1, 0.5)), uniform
+weights 1/N, [-6,6]^2 with a 64x64 P_DEG=2 mesh, dt = 0.02, Gonzalez on,
+Anderson depth 8, damping 0.7, tol 1e-12, abs_floor 0 (so tol*||v|| binds),
+N_QUAD 6. Markers are seeded synthetic data (numpy default_rng(42)).
+
+One "step" = one time step of the reference's loop (main.jl:226-300): the
+explicit predictor, step_anderson! to convergence, and the entropy S0 of the
+new state for the next step. `value` times the headline form (mixed: FP32 pair
+maps, FP64 exit Picard map) with inputs resident in HBM; `plain_fp64` times the
+plain FP64 form from the same state; `e2e` drives the headline form through the
+host-pointer C ABI with host<->device copies inside the timed region.
+Each timed step is bracketed by CUDA events on the library's stream; a 256 MB
+buffer is written between timed steps to flush L2.
+
+--impl reference times the CPU FP64 oracle (the reference's CPU algorithm,
+OpenMP over all host cores) on the same workload: one Picard map per step with
+the pair sum evaluated on a seeded sample of target rows and scaled to all rows,
+times the number of maps of a converged FP64 step.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import ctypes as C
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "collisionoperators.jl_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "ms/converged implicit step, Landau N=131k: mixed+learned vs plain FP64 GPU"
+UNIT = "ms/step"
+WORKLOAD = dict(name="landau_n131072_mesh64_dt0.02", N=131072, n_el=64, lo=-6.0, hi=6.0,
+                sx=1.0, sy=0.5, dt=0.02, m=8, damping=0.7, tol=1e-12, abs_floor=0.0,
+                max_iter=2000, seed=42)
+# maps per converged FP64 step of this workload, measured by the plain FP64
+# GPU solve (profiles/c3_fp64_step.md); used only when this run does not
+# measure it itself
+FP64_MAPS_FILE = os.path.join(ROOT, "profiles", "c3_fp64_step.md")
+
+
+def markers(cfg, seed):
+    rng = np.random.default_rng(seed)
+    N = cfg["N"]
+    v = np.zeros((N, 2), order="F")
+    v[:, 0] = cfg["sx"] * rng.standard_normal(N)
+    v[:, 1] = cfg["sy"] * rng.standard_normal(N)
+    w = np.full(N, 1.0 / N)
+    return v, w
+
+
+def bp_of(cfg):
+    return np.linspace(cfg["lo"], cfg["hi"], cfg["n_el"] + 1)
+
+
+# ---------------------------------------------------------------- clocks
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for r in csv.reader(f):
+                if len(r) >= 9:
+                    rows.append([x.strip() for x in r])
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ---------------------------------------------------------------- multi-GPU
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def aggregate(elapsed_ms: float, steps: int, world: int, group=None):
+    """Replicas: every rank runs the same workload on its own GPU; the job time
+    is the max over ranks, and the job's ms per step is that time over all
+    ranks' steps (weak scaling). Returns (job_ms_per_step, max_elapsed_ms)."""
+    t = elapsed_ms
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        x = torch.tensor([elapsed_ms], dtype=torch.float64,
+                         device="cuda" if dist.get_backend(group) == "nccl" else "cpu")
+        dist.all_reduce(x, op=dist.ReduceOp.MAX, group=group)
+        t = float(x.item())
+    return t / (steps * world), t
+
+
+# ---------------------------------------------------------------- CPU side
+
+def oracle_map_sample(cfg, v, w, rows_sample: int, threads: int):
+    """One Picard map of the CPU oracle at the full workload with the pair sum on
+    a seeded sample of target rows; returns (estimated ms per map, details)."""
+    import oracle
+    oracle.build()
+    bp = bp_of(cfg)
+    om = oracle.OracleMesh(bp, bp, 6)
+    o = oracle.Opts(model="landau", nthreads=threads)
+    dt = cfg["dt"]
+    N = cfg["N"]
+    # v_in: a perturbed state standing in for the predictor (same cost)
+    v_in = np.asfortranarray(v + 1e-3 * np.sin(np.arange(2 * N)).reshape(N, 2, order="F"))
+    t0 = time.perf_counter()
+    S0 = om.entropy(om.l2_project(v, w))
+    t_s0 = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    f_in = om.l2_project(v_in, w)          # Gonzalez projection of v_in
+    S1 = om.entropy(f_in)
+    vm = np.asfortranarray(0.5 * (v + v_in))
+    f = om.l2_project(vm, w)
+    L = om.mass_solve(om.compute_r(f))
+    G = om.compute_G(vm, L)
+    t_on = time.perf_counter() - t0
+    inside = np.all((vm > cfg["lo"]) & (vm < cfg["hi"]), axis=1)
+    n_in = int(inside.sum())
+    rng = np.random.default_rng(7)
+    rows = np.sort(rng.choice(np.flatnonzero(inside), size=min(rows_sample, n_in), replace=False))
+    t0 = time.perf_counter()
+    om.collision_rows(vm, w, G, rows, nthreads=threads)
+    t_pairs = time.perf_counter() - t0
+    per_map = (t_on + t_pairs * n_in / len(rows)) * 1e3
+    _ = (S0, S1, t_s0)
+    return per_map, dict(t_on_ms=t_on * 1e3, t_pairs_sample_ms=t_pairs * 1e3, rows=len(rows),
+                         n_in=n_in)
+
+
+def fp64_maps_from_profile():
+    try:
+        for line in open(FP64_MAPS_FILE):
+            if line.startswith("maps_per_step:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline(cfg, maps_per_step, maps_src, rows_sample=1024):
+    threads = os.cpu_count() or 1
+    v, w = markers(cfg, cfg["seed"])
+    per_map, d = oracle_map_sample(cfg, v, w, rows_sample, threads)
+    value = per_map * maps_per_step
+    sample = (f"one Picard map of the FP64 oracle at N={cfg['N']}: projection, quadrature, "
+              f"mass solves and grad-L in full ({d['t_on_ms']:.0f} ms), pair sum on "
+              f"{d['rows']} seeded target rows ({d['t_pairs_sample_ms']:.0f} ms) scaled to "
+              f"{d['n_in']} rows; x {maps_per_step:.1f} maps per converged FP64 step "
+              f"({maps_src})")
+    return dict(value=round(value, 1), unit=UNIT, cores=threads, kind="port", sample=sample,
+                per_map_ms=round(per_map, 1))
+
+
+# ---------------------------------------------------------------- GPU side
+
+def run_gpu(args, cfg):
+    import torch
+
+    world, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import collops as co
+    lib = co.load_library()
+    N, dt = cfg["N"], cfg["dt"]
+    bp = bp_of(cfg)
+    p = co.SimParameters(bp1=bp, bp2=bp, m_anderson=cfg["m"], damping=cfg["damping"],
+                         tol=cfg["tol"], abs_floor=cfg["abs_floor"], max_iter=cfg["max_iter"])
+    ws = co.build_workspace(p, device=local)
+    h = ws.h
+    sptr = C.c_void_p()
+    lib.co_ctx_stream(h, C.byref(sptr))
+    stream = torch.cuda.ExternalStream(sptr.value)
+
+    peak32, peak64 = C.c_double(), C.c_double()
+    lib.co_measure_fma_peak(local, 0, C.byref(peak32))
+    lib.co_measure_fma_peak(local, 1, C.byref(peak64))
+
+    v_np, w_np = markers(cfg, cfg["seed"] + rank)
+    dev = torch.device("cuda", local)
+    v = torch.from_numpy(np.ascontiguousarray(v_np.T)).to(dev)      # (2, N) = Julia N x 2
+    w = torch.from_numpy(w_np).to(dev)
+    v1 = torch.empty_like(v)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def opts(prec):
+        return p.opts(precision=co.CO_PREC_MIXED if prec == "mixed" else co.CO_PREC_FP64,
+                      mixed_floor=args.mixed_floor)
+
+    def entropy(x):
+        S = C.c_double()
+        co._check(lib.co_entropy_of_markers_dev(h, x.data_ptr(), w.data_ptr(), N, C.byref(S)),
+                  "co_entropy_of_markers_dev")
+        return S.value
+
+    dopt = co.CoDefectOpts(args.dc_eta, args.dc_max_inner, args.dc_stag_window, 0.5, 0)
+
+    def one_step(x, S0, prec, solver=None):
+        """predictor + the implicit solve (+ S of the new state); returns new x, S, info."""
+        solver = solver or args.solver
+        o = opts(prec)
+        co._check(lib.co_predictor_dev(h, C.byref(o), v1.data_ptr(), x.data_ptr(), w.data_ptr(),
+                                       N, dt), "co_predictor_dev")
+        it, nrs = C.c_int(), C.c_int()
+        res, r0 = C.c_double(), C.c_double()
+        if solver == "defect":
+            o.stag_rel_tol = 0.1
+            co._check(lib.co_step_defect_dev(h, C.byref(o), C.byref(dopt), v1.data_ptr(),
+                                             x.data_ptr(), w.data_ptr(), N, S0, dt, C.byref(it),
+                                             C.byref(res), C.byref(nrs), C.byref(r0)),
+                      "co_step_defect_dev")
+        else:
+            co._check(lib.co_step_anderson_dev(h, C.byref(o), v1.data_ptr(), x.data_ptr(),
+                                               w.data_ptr(), N, S0, dt, C.byref(it),
+                                               C.byref(res), C.byref(nrs), C.byref(r0)),
+                      "co_step_anderson_dev")
+        S1 = entropy(v1)
+        return v1.clone(), S1, (it.value, res.value, nrs.value, r0.value)
+
+    def fp64_residual(x_new, x_old, S_old):
+        """||G64(x) - x|| of a returned state (one FP64 Picard map, untimed)."""
+        o = opts("fp64")
+        out = np.zeros((N, 2), order="F")
+        xn = np.asfortranarray(x_new.cpu().numpy().T)
+        xo = np.asfortranarray(x_old.cpu().numpy().T)
+        co._check(lib.co_picard_map(h, C.byref(o), co._p(out), co._p(xn), co._p(xo),
+                                    co._p(w.cpu().numpy()), N, S_old, dt), "co_picard_map")
+        return float(np.linalg.norm(out - xn))
+
+    def timed_steps(x, S0, prec, k, solver=None):
+        times, infos = [], []
+        for _ in range(k):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            x, S0, info = one_step(x, S0, prec, solver)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+            infos.append(info)
+        return x, S0, times, infos
+
+    S0 = entropy(v)
+    x = v.clone()
+    # warm-up (advances the state)
+    for _ in range(args.warmup):
+        x, S0, _info = one_step(x, S0, args.form)
+    x_start, S_start = x.clone(), S0
+
+    # ---- timed headline form
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    lib.co_profile(h, 1)
+    n_launch0 = ws.launch_count()
+    x_end, S_end, times, infos = timed_steps(x_start.clone(), S_start, args.form, args.steps)
+    n_launch = ws.launch_count() - n_launch0
+    prof = co.CoProfile()
+    lib.co_profile_read(h, C.byref(prof))
+    lib.co_profile(h, 0)
+    clk = clocks.stop()
+    elapsed = float(sum(times))
+    if world > 1:
+        dist.barrier()
+    job_ms, max_elapsed = aggregate(elapsed, args.steps, world)
+
+    # ---- accuracy and the plain FP64 form from the same start state
+    plain = None
+    acc = None
+    if args.plain_steps > 0:
+        lib.co_profile(h, 1)
+        xp, Sp, tp, ip = timed_steps(x_start.clone(), S_start, "fp64", args.plain_steps,
+                                     solver="anderson")
+        prof64 = co.CoProfile()
+        lib.co_profile_read(h, C.byref(prof64))
+        lib.co_profile(h, 0)
+        # one headline step from the same start for the velocity comparison
+        xm, Sm, _info = one_step(x_start.clone(), S_start, args.form)
+        x0 = x_start.cpu().numpy()
+        a64, am = xp.cpu().numpy(), xm.cpu().numpy()
+        wn = w.cpu().numpy()
+        if args.plain_steps == 1:
+            def drift(a):
+                dP = np.abs((wn * (a - x0)).sum(1)).max()
+                E0 = 0.5 * (wn * (x0 ** 2).sum(0)).sum()
+                dE = abs(0.5 * (wn * (a ** 2).sum(0)).sum() - E0) / E0
+                return float(dP), float(dE)
+            acc = dict(vel_diff_vs_plain_fp64=float(np.abs(am - a64).max() / np.abs(a64).max()),
+                       fp64_map_residual_headline=fp64_residual(xm, x_start, S_start),
+                       fp64_map_residual_plain=fp64_residual(xp, x_start, S_start),
+                       momentum_drift_mixed=drift(am)[0], energy_drift_rel_mixed=drift(am)[1],
+                       momentum_drift_fp64=drift(a64)[0], energy_drift_rel_fp64=drift(a64)[1])
+        plain = dict(ms_per_step=round(statistics.mean(tp), 1), steps=len(tp),
+                     iterations=[i[0] for i in ip], residuals=[i[1] for i in ip],
+                     pair64_ms_avg=(prof64.pair64_ms / max(1, prof64.pair64_launches)))
+
+    # ---- e2e through the host-pointer C ABI
+    e2e = None
+    if args.e2e_steps > 0:
+        xh = np.asfortranarray(x_start.cpu().numpy().T)  # N x 2 column-major host array
+        wh = w.cpu().numpy().copy()
+        f = np.zeros(ws.n_dofs)
+        Sh = S_start
+        ets = []
+        o = opts(args.form)
+        for _ in range(args.e2e_steps):
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            v1h = np.zeros((N, 2), order="F")
+            co._check(lib.co_predictor(h, C.byref(o), co._p(v1h), co._p(xh), co._p(wh), N, dt),
+                      "co_predictor")
+            it, nrs = C.c_int(), C.c_int()
+            res, r0 = C.c_double(), C.c_double()
+            if args.solver == "defect":
+                o.stag_rel_tol = 0.1
+                co._check(lib.co_step_defect(h, C.byref(o), C.byref(dopt), co._p(v1h), co._p(xh),
+                                             co._p(wh), N, Sh, dt, C.byref(it), C.byref(res),
+                                             C.byref(nrs), C.byref(r0)), "co_step_defect")
+            else:
+                co._check(lib.co_step_anderson(h, C.byref(o), co._p(v1h), co._p(xh), co._p(wh),
+                                               N, Sh, dt, C.byref(it), C.byref(res),
+                                               C.byref(nrs), C.byref(r0)), "co_step_anderson")
+            co._check(lib.co_l2_project(h, co._p(v1h), co._p(wh), co._p(f), N), "co_l2_project")
+            Sbuf = np.zeros(1)
+            co._check(lib.co_entropy(h, co._p(f), co._p(Sbuf)), "co_entropy")
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ets.append(e0.elapsed_time(e1))
+            xh, Sh = v1h, float(Sbuf[0])
+        nd = ws.n_dofs
+        h2d = 8 * (3 * N + 5 * N + 3 * N + nd)   # predictor v,w; step v1,v0,w; project v,w; f
+        d2h = 8 * (2 * N + 2 * N + nd + 1)       # predictor v1; step v1; f; S
+        e2e_job, _ = aggregate(float(sum(ets)), len(ets), world)
+        e2e = dict(value=round(e2e_job, 2), unit=UNIT, h2d_bytes_per_step=h2d,
+                   d2h_bytes_per_step=d2h)
+
+    # ---- roofline of the dominant pair kernel
+    def roof(ms, launches, pairs, peak, kind):
+        if launches == 0:
+            return None
+        avg_ms = ms / launches
+        flops = 23.0 * pairs / launches            # 23 algorithmic flops per ordered pair
+        achieved = flops / (avg_ms * 1e-3) / 1e12
+        pk = peak / 1e12
+        return {"bound": kind, "achieved": round(achieved, 3), "peak": round(pk, 3),
+                "unit": "TFLOP/s", "frac": round(achieved / pk, 4), "traffic": None,
+                "kernel": "k_pair32" if kind == "fp32" else "k_pair64<false>",
+                "avg_launch_ms": round(avg_ms, 3), "launches": launches,
+                "pairs_per_launch": pairs / launches,
+                "peak_source": "measured in this run: FMA-chain kernel (co_measure_fma_peak), "
+                               "2 flops per FMA; no FP32/FP64 SIMT figure in MEASURED_PEAKS.json"}
+
+    r32 = roof(prof.pair32_ms, prof.pair32_launches, prof.pair32_pairs, peak32.value, "fp32")
+    r64 = roof(prof.pair64_ms, prof.pair64_launches, prof.pair64_pairs, peak64.value, "fp64")
+    dominant = r32 if (prof.pair32_ms >= prof.pair64_ms and r32) else r64
+    traffic = load_traffic()
+    if dominant and traffic.get(dominant["kernel"]) is not None:
+        dominant["traffic"] = traffic[dominant["kernel"]]
+
+    maps_fp64 = None
+    maps_src = None
+    if plain:
+        maps_fp64 = statistics.mean(plain["iterations"]) + 1
+        maps_src = "measured by the plain FP64 GPU step in this run (iterations + predictor)"
+    else:
+        mf = fp64_maps_from_profile()
+        if mf:
+            maps_fp64, maps_src = mf, "from " + os.path.relpath(FP64_MAPS_FILE, ROOT)
+    cpu = None
+    if rank == 0 and world == 1 and args.cpu_baseline and maps_fp64:
+        cpu = cpu_baseline(cfg, maps_fp64, maps_src, rows_sample=args.cpu_rows)
+
+    line = {
+        "metric": METRIC, "value": round(job_ms, 2), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(job_ms, 2),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32 pair arithmetic + fp64" if args.form == "mixed" else "fp64",
+        "data": "synthetic: seeded anisotropic Gaussian markers (numpy default_rng)",
+        "config": {"workload": cfg["name"], "form": args.form, "solver": args.solver, "N": N,
+                   "mesh": f"{cfg['n_el']}x{cfg['n_el']} P2 on [{cfg['lo']},{cfg['hi']}]^2",
+                   "dt": dt, "anderson_m": cfg["m"], "damping": cfg["damping"],
+                   "tol": cfg["tol"], "abs_floor": cfg["abs_floor"], "gonzalez": True,
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "256 MB buffer written between timed steps"},
+        "step_ms": [round(t, 1) for t in times],
+        "iterations": [i[0] for i in infos], "residuals": [i[1] for i in infos],
+        "inner_or_restarts": [i[2] for i in infos],
+        "maps": {"fp32": prof.maps32, "fp64": prof.maps64},
+        "plain_fp64": plain, "accuracy": acc,
+        "roofline": dominant, "roofline_fp64": r64,
+        "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": int(n_launch),
+    }
+    if plain:
+        line["speedup_vs_plain_fp64"] = round(plain["ms_per_step"] / job_ms, 2)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def load_traffic():
+    """DRAM bytes per launch from the committed ncu summaries (profiles/*.md lines
+    'traffic_bytes_per_launch <kernel>: <bytes>')."""
+    out = {}
+    d = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(d):
+        return out
+    for fn in os.listdir(d):
+        if not fn.endswith(".md"):
+            continue
+        for line in open(os.path.join(d, fn)):
+            if line.startswith("traffic_bytes_per_launch "):
+                k, val = line[len("traffic_bytes_per_launch "):].split(":")
+                try:
+                    out[k.strip()] = float(val)
+                except ValueError:
+                    pass
+    return out
+
+
+def run_reference(args, cfg):
+    world, rank, _ = dist_info()
+    if rank != 0:
+        return
+    maps = fp64_maps_from_profile()
+    src = "from " + os.path.relpath(FP64_MAPS_FILE, ROOT)
+    if maps is None:
+        print(json.dumps({"impl": "reference", "metric": METRIC,
+                          "unavailable": "maps per converged FP64 step not yet measured"}))
+        return
+    vals = []
+    info = None
+    for k in range(args.warmup + args.steps):
+        info = cpu_baseline(cfg, maps, src, rows_sample=args.cpu_rows)
+        if k >= args.warmup:
+            vals.append(info["value"])
+    value = statistics.mean(vals)
+    line = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "impl": "reference",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(value, 1), "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp64",
+            "data": "synthetic: seeded anisotropic Gaussian markers (numpy default_rng)",
+            "config": {"workload": cfg["name"], "form": "reference CPU FP64 (oracle port)",
+                       "N": cfg["N"]},
+            "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": info["cores"],
+                             "kind": "port", "sample": info["sample"]},
+            "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--form", choices=["mixed", "fp64"], default="mixed")
+    ap.add_argument("--solver", choices=["defect", "anderson"], default="defect")
+    ap.add_argument("--dc-eta", type=float, default=0.05)
+    ap.add_argument("--dc-max-inner", type=int, default=60)
+    ap.add_argument("--dc-stag-window", type=int, default=5)
+    ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--mixed-floor", type=float, default=0.0)
+    ap.add_argument("--cpu-rows", type=int, default=1024)
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--N", type=int, default=None, help="override the marker count (tests)")
+    args = ap.parse_args(argv)
+    args.warmup = max(args.warmup, 0)
+    cfg = dict(WORKLOAD)
+    if args.N:
+        cfg["N"] = args.N
+        cfg["name"] = f"landau_n{args.N}_mesh64_dt0.02"
+    if args.impl == "reference":
+        run_reference(args, cfg)
+    else:
+        run_gpu(args, cfg)
+
+
+if __name__ == "__main__":
+    main()

@@ -23,7 +23,8 @@ __all__ = [
     "CollopsError", "SimParameters", "parse_overrides", "Workspace", "build_workspace",
     "compute_collision_gpu", "compute_collision_gpu32", "compute_collision_metric_gpu",
     "l2_project_gpu", "compute_G_gpu", "eval_loggrad_gpu", "compute_r_gpu",
-    "compute_entropy_gpu", "mass_solve_gpu", "picard_map", "step_anderson", "predictor",
+    "compute_entropy_gpu", "mass_solve_gpu", "picard_map", "step_anderson", "step_defect",
+    "predictor",
     "enable_gpu", "Hooks", "library_path", "load_library",
 ]
 
@@ -36,7 +37,7 @@ _ip = C.POINTER(C.c_int)
 
 CO_MODEL_LANDAU, CO_MODEL_LB = 0, 1
 CO_PREC_FP64, CO_PREC_MIXED = 0, 1
-CO_FLAG_LOGSQ, CO_FLAG_FP32_PAIR = 1, 2
+CO_FLAG_LOGSQ, CO_FLAG_FP32_PAIR, CO_FLAG_ONESIDED = 1, 2, 4
 
 
 class CollopsError(RuntimeError):
@@ -59,6 +60,20 @@ class CoOpts(C.Structure):
         ("restart_factor", C.c_double), ("damping", C.c_double),
         ("reg_factor", C.c_double), ("precision", C.c_int), ("mixed_floor", C.c_double),
     ]
+
+
+class CoProfile(C.Structure):
+    """co_profile_t of include/collops.h."""
+    _fields_ = [("pair64_ms", C.c_double), ("pair64_launches", C.c_ulonglong),
+                ("pair64_pairs", C.c_double), ("pair32_ms", C.c_double),
+                ("pair32_launches", C.c_ulonglong), ("pair32_pairs", C.c_double),
+                ("maps64", C.c_ulonglong), ("maps32", C.c_ulonglong)]
+
+
+class CoDefectOpts(C.Structure):
+    """co_defect_opts of include/collops.h."""
+    _fields_ = [("eta", C.c_double), ("max_inner", C.c_int), ("stag_window", C.c_int),
+                ("fp32_stall", C.c_double), ("metric64", C.c_int)]
 
 
 # (name, restype, argtypes) of every entry point in include/collops.h
@@ -84,12 +99,21 @@ _SIGNATURES = {
     "co_step_anderson_dev": (C.c_int, [C.c_void_p, C.POINTER(CoOpts), C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_int, C.c_double, C.c_double, _ip, _dp,
                                        _ip, _dp]),
+    "co_step_defect": (C.c_int, [C.c_void_p, C.POINTER(CoOpts), C.POINTER(CoDefectOpts), _dp,
+                                 _dp, _dp, C.c_int, C.c_double, C.c_double, _ip, _dp, _ip, _dp]),
+    "co_step_defect_dev": (C.c_int, [C.c_void_p, C.POINTER(CoOpts), C.POINTER(CoDefectOpts),
+                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double,
+                                     C.c_double, _ip, _dp, _ip, _dp]),
     "co_predictor": (C.c_int, [C.c_void_p, C.POINTER(CoOpts), _dp, _dp, _dp, C.c_int,
                                C.c_double]),
     "co_predictor_dev": (C.c_int, [C.c_void_p, C.POINTER(CoOpts), C.c_void_p, C.c_void_p,
                                    C.c_void_p, C.c_int, C.c_double]),
     "co_entropy_of_markers_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, _dp]),
     "co_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_ulonglong)]),
+    "co_ctx_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "co_profile": (C.c_int, [C.c_void_p, C.c_int]),
+    "co_profile_read": (C.c_int, [C.c_void_p, C.POINTER(CoProfile)]),
+    "co_measure_fma_peak": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
 }
 
 
@@ -160,9 +184,11 @@ class SimParameters:
     gpu_fp32: bool = False
     suffix: str = "anderson"
     seed: int = 42
-    # build-specific: precision form of the implicit solve ("fp64" | "mixed")
+    # build-specific: precision form of the implicit solve ("fp64" | "mixed"),
+    # and the one-sided pair kernels in place of the symmetric ones
     precision: str = "fp64"
     mixed_floor: float = 0.0
+    pair_onesided: bool = False
 
     def opts(self, **kw) -> CoOpts:
         """co_opts for step_anderson!/picard_map! from these parameters."""
@@ -259,7 +285,8 @@ class Workspace:
         self.p = p
         self.bp1 = np.ascontiguousarray(p.bp1, dtype=np.float64)
         self.bp2 = np.ascontiguousarray(p.bp2, dtype=np.float64)
-        flags = (CO_FLAG_LOGSQ if p.use_logsq else 0) | (CO_FLAG_FP32_PAIR if p.gpu_fp32 else 0)
+        flags = ((CO_FLAG_LOGSQ if p.use_logsq else 0) | (CO_FLAG_FP32_PAIR if p.gpu_fp32 else 0)
+                 | (CO_FLAG_ONESIDED if p.pair_onesided else 0))
         h = C.c_void_p()
         self.h = None
         _check(self.lib.co_ctx_create(_p(self.bp1), len(self.bp1), _p(self.bp2), len(self.bp2),
@@ -416,6 +443,28 @@ def step_anderson(ws: Workspace, v1, v0, w_parts, S0: float, dt: float, *, m: in
                                    _p(_vec(w_parts, N, "w_parts")), N, S0, dt, C.byref(it),
                                    C.byref(res), C.byref(nrs), C.byref(r0)), "co_step_anderson")
     return it.value, res.value, nrs.value, r0.value
+
+
+def step_defect(ws: Workspace, v1, v0, w_parts, S0: float, dt: float, *, m: int = 8,
+                max_iter: int = 2000, tol: float = 1e-12, abs_floor: float = 1e-7,
+                damping: float = 0.7, eta: float = 0.05, max_inner: int = 60,
+                stag_window: int = 5, stag_rel_tol: float = 0.1, use_gonzalez: bool = True,
+                precision: str = "fp64", metric64: bool = True, fp32_stall: float = 0.5):
+    """step_defect! (solver.jl:569-634) on the device; v1 (guess) is overwritten with
+    the solution. Returns (outer_iterations, residual, inner_iterations, initial_residual)."""
+    v0 = _markers(v0, name="v0")
+    N = v0.shape[0]
+    v1 = _out(v1, (N, 2), "v1")
+    o = ws.p.opts(m=m, max_iter=max_iter, tol=tol, abs_floor=abs_floor, damping=damping,
+                  stag_rel_tol=stag_rel_tol, use_gonzalez=int(use_gonzalez),
+                  precision=CO_PREC_MIXED if precision == "mixed" else CO_PREC_FP64)
+    d = CoDefectOpts(eta, max_inner, stag_window, fp32_stall, int(metric64))
+    it, inner = C.c_int(), C.c_int()
+    res, r0 = C.c_double(), C.c_double()
+    _check(ws.lib.co_step_defect(ws.h, C.byref(o), C.byref(d), _p(v1), _p(v0),
+                                 _p(_vec(w_parts, N, "w_parts")), N, S0, dt, C.byref(it),
+                                 C.byref(res), C.byref(inner), C.byref(r0)), "co_step_defect")
+    return it.value, res.value, inner.value, r0.value
 
 
 def predictor(ws: Workspace, v1, v_parts, w_parts, dt: float, precision: str = "fp64") -> None:

@@ -179,9 +179,11 @@ static void free_ctx(co_ctx *c) {
                     c->mb.cell, c->mb.inv, c->mb.xi, c->mb.perm, c->mb.scell, c->mb.sw,
                     c->mb.sphi, c->mb.px, c->mb.pg, c->mb.pw, c->mb.pf_x, c->mb.pf_g, c->mb.pf_w,
                     c->mb.pdot, c->mb.pA, c->mb.part, c->mb.hist, c->mb.hoff, c->mb.count,
-                    c->mb.cstart, c->mb.red, c->mb.dF, c->mb.dG};
+                    c->mb.cstart, c->mb.red, c->mb.dF, c->mb.dG, c->mb.Gk, c->mb.Phi,
+                    c->mb.Adef, c->st2};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    co_prof_free(c);
     if (c->st_host) cudaFreeHost(c->st_host);
     if (c->stream) cudaStreamDestroy(c->stream);
     free(c);
@@ -211,6 +213,7 @@ extern "C" int co_ctx_create(const double *bp1, int nb1, const double *bp2, int 
     c->n_dofs = c->nd1 * c->nd2;
     c->n_el = c->n1 * c->n2;
     c->nq = n_quad;
+    c->pair_symmetric = (flags & CO_FLAG_ONESIDED) ? 0 : 1;
     c->lo1 = bp1[0];
     c->hi1 = bp1[c->n1];
     c->lo2 = bp2[0];
@@ -488,9 +491,13 @@ extern "C" int co_picard_map(co_ctx *c, const co_opts *o, double *v_out, const d
     RC(h2d(c, b.vin, v_in, 2 * (size_t)N));
     RC(h2d(c, b.v0, v0, 2 * (size_t)N));
     RC(h2d(c, b.w, w, N));
+    CO_CK(cudaMemsetAsync(&c->st->error, 0, sizeof(int), c->stream));
     RC(co_picard_map_dev(c, o, o->precision, b.Gv, b.vin, b.v0, b.w, N, S0, dt, 0));
     RC(d2h(c, v_out, b.Gv, 2 * (size_t)N));
-    return finish(c);
+    CO_CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(co_solver_state), cudaMemcpyDeviceToHost,
+                          c->stream));
+    RC(finish(c));
+    return c->st_host->error ? c->st_host->error : CO_OK;
 }
 
 extern "C" int co_step_anderson(co_ctx *c, const co_opts *o, double *v1, const double *v0,
@@ -580,5 +587,53 @@ extern "C" int co_entropy_of_markers_dev(co_ctx *c, const double *v, const doubl
     RC(co_entropy_parts_dev(c, c->f));
     RC(co_entropy_finalize_dev(c, c->y));
     RC(d2h(c, S, c->y, 1));
+    return finish(c);
+}
+
+static int check_defect(const co_opts *o, const co_defect_opts *d) {
+    int rc = check_opts(o);
+    if (rc) return rc;
+    if (!d || o->model != CO_MODEL_LANDAU || d->max_inner < 1 || d->stag_window < 1 ||
+        !(d->eta > 0))
+        return CO_ERR_ARG;
+    return CO_OK;
+}
+
+extern "C" int co_step_defect(co_ctx *c, const co_opts *o, const co_defect_opts *d, double *v1,
+                              const double *v0, const double *w, int N, double S0, double dt,
+                              int *outer, double *res, int *inner, double *r0) {
+    ENTER(c);
+    RC(check_defect(o, d));
+    if (N < 0 || (N > 0 && (!v1 || !v0 || !w))) return CO_ERR_ARG;
+    if (N > 0 && (!all_finite(v1, 2 * (size_t)N) || !all_finite(v0, 2 * (size_t)N) ||
+                  !all_finite(w, N)))
+        return CO_ERR_NONFINITE;
+    RC(co_ensure_capacity(c, N, o->m));
+    co_bufs &b = c->mb;
+    RC(h2d(c, b.v1, v1, 2 * (size_t)N));
+    RC(h2d(c, b.v0, v0, 2 * (size_t)N));
+    RC(h2d(c, b.w, w, N));
+    RC(co_step_defect_buffers(c, o, d, N, S0, dt, outer, res, inner, r0));
+    RC(d2h(c, v1, b.v1, 2 * (size_t)N));
+    return finish(c);
+}
+
+extern "C" int co_step_defect_dev(co_ctx *c, const co_opts *o, const co_defect_opts *d,
+                                  double *v1, const double *v0, const double *w, int N, double S0,
+                                  double dt, int *outer, double *res, int *inner, double *r0) {
+    ENTER(c);
+    RC(check_defect(o, d));
+    if (N < 0 || (N > 0 && (!v1 || !v0 || !w))) return CO_ERR_ARG;
+    RC(co_ensure_capacity(c, N, o->m));
+    co_bufs &b = c->mb;
+    size_t n2 = 2 * (size_t)N * sizeof(double);
+    if (N > 0) {
+        CO_CK(cudaMemcpyAsync(b.v1, v1, n2, cudaMemcpyDeviceToDevice, c->stream));
+        CO_CK(cudaMemcpyAsync(b.v0, v0, n2, cudaMemcpyDeviceToDevice, c->stream));
+        CO_CK(cudaMemcpyAsync(b.w, w, (size_t)N * sizeof(double), cudaMemcpyDeviceToDevice,
+                              c->stream));
+    }
+    RC(co_step_defect_buffers(c, o, d, N, S0, dt, outer, res, inner, r0));
+    if (N > 0) CO_CK(cudaMemcpyAsync(v1, b.v1, n2, cudaMemcpyDeviceToDevice, c->stream));
     return finish(c);
 }

@@ -29,6 +29,7 @@ struct co_solver_state {
     int k;               // current iteration (1-based)
     int history, slot;   // Anderson window (solver.jl:320-321)
     int n_restart;
+    int k64;             // defect correction: FP64 outer maps so far
     int done;            // 0 running, 1 converged, 2 stagnated, 3 max_iter
     int path;            // 0 damped Picard, 1 Anderson, for the current k
     int improved;        // nrm_r < nrm_best at the current k
@@ -70,6 +71,8 @@ struct co_bufs {
     // Anderson window
     double *dF, *dG;     // 2N x m each
     int m_cap;
+    // defect correction (allocated on first use)
+    double *Gk, *Phi, *Adef;
 };
 
 struct co_ctx {
@@ -91,13 +94,18 @@ struct co_ctx {
     double *Ep;              // element entropy partials [n_el]
     co_bufs mb;
     co_solver_state *st;     // device state
+    co_solver_state *st2;    // inner-solve state of the defect correction
     co_solver_state *st_host;  // pinned mirror
     double *hstage;          // pinned host staging (grows)
     size_t hstage_cap;
-    int pair_split_fp64, pair_split_fp32;  // autotuned split factors (0 = auto)
+    int pair_split_fp64, pair_split_fp32;  // split factors of the plain kernels (0 = auto)
+    int pair_symmetric;      // 1: Newton's-third-law kernels (default), 0: one-sided
     int nsm;
     // launch counter (kernels of this library launched through the context)
     unsigned long long launches;
+    // pair-kernel profiling (co_prof.cu)
+    struct co_prof *prof;
+    unsigned long long maps64, maps32;
 };
 
 // ------------------------------------------------------------- helpers
@@ -131,8 +139,20 @@ int co_pair_fp32(co_ctx *c, int M);                    // packed FP32 -> pdot
 int co_pack_landau(co_ctx *c, int N, int Mub, int precision, int gonzalez);
 int co_pack_plain(co_ctx *c, int N, int Mub, int precision, const double *x, const double *G);
 int co_unpack_A(co_ctx *c, int N, double *A);
+int co_metric32(co_ctx *c, int Mub);   // FP32 metric A (3 x ld in pA) from pf_x/pf_w
+int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *dopt, int N,
+                           double S0, double dt, int *outer, double *res, int *inner, double *r0);
+#define CO_PREC_BOTH 2                  // pack both FP64 and FP32 operands
 int co_unpack_update(co_ctx *c, int N, double dt, double *Gv, const double *v0,
                      const double *v1, double *r, double *red);
+
+// ------------------------------------------------------------- profiling
+// (co_prof.cu) -- event pairs around pair-kernel launches, collected after
+// stream synchronisation
+void co_prof_begin(co_ctx *c, int fp64);
+void co_prof_end(co_ctx *c);
+void co_prof_collect(co_ctx *c);
+void co_prof_free(co_ctx *c);
 
 // ------------------------------------------------------------- solver stage
 // (co_solver.cu)

@@ -234,6 +234,289 @@ k_pair32(const float4 *__restrict__ pfx, const float4 *__restrict__ pfg,
     }
 }
 
+// ------------------------------------------------------------------ metric (FP32)
+//
+// A_g = sum_a w_a U(v_g - v_a), U(z) = (I - z z^T/|z|^2)/|z|  (functions.jl:278-281),
+// evaluated in FP32 on the head parts of the packed operands. Used only as the
+// frozen metric of the defect-correction inner model (solver.jl:585-595), where
+// it shapes the convergence rate but not the fixed point: the outer residual is
+// always an FP64 (or, in the mixed form, FP32-then-FP64) Picard map.
+__global__ void __launch_bounds__(PAIR_TPB)
+k_metric32(const float4 *__restrict__ pfx, const float *__restrict__ pfw,
+           const int *__restrict__ Mp, double *__restrict__ out, size_t ld) {
+    __shared__ float2 sx[PAIR32_TILE];
+    __shared__ float sw[PAIR32_TILE];
+    const int M = *Mp;
+    const int g0 = blockIdx.x * PAIR_TPB;
+    if (g0 >= M) return;
+    const int g = g0 + threadIdx.x;
+    float2 xg = make_float2(0.f, 0.f);
+    if (g < M) {
+        float4 t = pfx[g];
+        xg = make_float2(t.x + t.z, t.y + t.w);
+    }
+    double A11 = 0.0, A12 = 0.0, A22 = 0.0;
+    for (int base = 0; base < M; base += PAIR32_TILE) {
+        for (int k = threadIdx.x; k < PAIR32_TILE; k += PAIR_TPB) {
+            int a = base + k;
+            if (a < M) {
+                float4 t = pfx[a];
+                sx[k] = make_float2(t.x + t.z, t.y + t.w);
+                sw[k] = pfw[a];
+            } else {
+                sx[k] = make_float2(1e3f, 1e3f);
+                sw[k] = 0.f;
+            }
+        }
+        __syncthreads();
+        float a11 = 0.f, a12 = 0.f, a22 = 0.f;
+#pragma unroll 8
+        for (int k = 0; k < PAIR32_TILE; k++) {
+            float d1 = xg.x - sx[k].x, d2 = xg.y - sx[k].y;
+            float r2 = fmaf(d2, d2, d1 * d1);
+            float y = rsqrtf(r2);
+            y = r2 >= 1e-24f ? y : 0.f;
+            float s = sw[k] * y;
+            float y2 = y * y;
+            a11 = fmaf(s, fmaf(-d1 * d1, y2, 1.f), a11);
+            a12 = fmaf(-s, d1 * d2 * y2, a12);
+            a22 = fmaf(s, fmaf(-d2 * d2, y2, 1.f), a22);
+        }
+        A11 += (double)a11;
+        A12 += (double)a12;
+        A22 += (double)a22;
+        __syncthreads();
+    }
+    if (g < M) {
+        out[g] = A11;
+        out[ld + g] = A12;
+        out[2 * ld + g] = A22;
+    }
+}
+
+// ------------------------------------------------------------------ symmetric
+//
+// Newton's third law for the pair sum: with d = v_g - v_a and g = G_a - G_g,
+// the ordered pair (a, g) sees d' = -d and g' = -g, so its term is
+// w_g U(d)(-g)/|d| = -w_g u with u = U(d) g / |d| the unweighted term of
+// (g, a). One evaluation of u serves both targets.
+//
+// Tiles of ST = 128 sorted markers; tile pairs (I, J = I + k mod nt) for
+// k = 0..H (H = nt/2; for even nt the k = H pairs are taken once, I < nt/2),
+// so every unordered tile pair appears exactly once and every row I has the
+// same work. A block owns I and a chunk of KC consecutive k. Inside a tile
+// pair the 4 warps take the 4 source sub-tiles in rotation (one warp per
+// sub-tile per round); within a warp, lane l pairs its target with source
+// (l + q) mod 32 at step q and passes the source's accumulator to lane l - 1
+// with a shuffle, so each source accumulator has one owner at every step. The
+// target side accumulates in registers across the chunk (gpart); the source
+// side of each tile pair is written to its own slot (apart) and everything is
+// summed afterwards in a fixed order: bitwise reproducible.
+//
+// FP64 body: 19 FP64 instructions for u + 4 FMAs for the two accumulations =
+// 23 per unordered pair, 11.5 per ordered pair (20 in k_pair64).
+#define ST 128
+
+__device__ __forceinline__ void pair_u64(double d1, double d2, double g1, double g2, double &u1,
+                                         double &u2) {
+    double r2 = d1 * d1;
+    r2 = fma(d2, d2, r2);
+    bool ok = __double_as_longlong(r2) >= CO_R2_MIN_BITS;
+    double xr = ok ? r2 : 1.0;
+    double y = rsqrt_seed64(xr);
+    double t = xr * y;
+    double e = fma(-t, y, 1.0);
+    double p = fma(0.375, e, 0.5);
+    double ye = y * e;
+    y = fma(ye, p, y);
+    double dg = d1 * g1;
+    dg = fma(d2, g2, dg);
+    double y2 = y * y;
+    double cc = dg * y2;
+    double t1 = fma(-d1, cc, g1);
+    double t2 = fma(-d2, cc, g2);
+    double ym = ok ? y : 0.0;
+    u1 = t1 * ym;
+    u2 = t2 * ym;
+}
+
+__device__ __forceinline__ bool sym_skip(int nt, int H, int I, int k) {
+    return k > 0 && (nt & 1) == 0 && k == H && I >= nt / 2;
+}
+
+__global__ void __launch_bounds__(ST)
+k_pair64_sym(const double2 *__restrict__ px, const double2 *__restrict__ pg,
+             const double *__restrict__ pw, int nt, int H, int KC,
+             double *__restrict__ gpart, double *__restrict__ apart) {
+    __shared__ double2 sx[ST], sg[ST];
+    __shared__ double sw[ST];
+    __shared__ double2 sacc[ST];
+    const int I = blockIdx.x % nt, chunk = blockIdx.x / nt;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const double2 xg = px[I * ST + tid], Gg = pg[I * ST + tid];
+    const double wg = pw[I * ST + tid];
+    double ga1 = 0.0, ga2 = 0.0;
+    const int k0 = chunk * KC, k1 = min(H + 1, k0 + KC);
+    for (int k = k0; k < k1; k++) {
+        if (sym_skip(nt, H, I, k)) continue;
+        const int J = (I + k) % nt;
+        __syncthreads();
+        sx[tid] = px[J * ST + tid];
+        sg[tid] = pg[J * ST + tid];
+        sw[tid] = pw[J * ST + tid];
+        sacc[tid] = make_double2(0.0, 0.0);
+        __syncthreads();
+        if (k == 0) {  // diagonal tile: ordered pairs, self excluded by the guard
+#pragma unroll 4
+            for (int a = 0; a < ST; a++) {
+                double u1, u2;
+                double2 xa = sx[a], Ga = sg[a];
+                pair_u64(xg.x - xa.x, xg.y - xa.y, Ga.x - Gg.x, Ga.y - Gg.y, u1, u2);
+                ga1 = fma(sw[a], u1, ga1);
+                ga2 = fma(sw[a], u2, ga2);
+            }
+            continue;
+        }
+        for (int r = 0; r < 4; r++) {
+            const int base = ((warp + r) & 3) * 32;
+            double2 a0 = sacc[base + lane];
+            double a1 = a0.x, a2 = a0.y;
+#pragma unroll 4
+            for (int q = 0; q < 32; q++) {
+                const int ai = base + ((lane + q) & 31);
+                double2 xa = sx[ai], Ga = sg[ai];
+                double wa = sw[ai];
+                double u1, u2;
+                pair_u64(xg.x - xa.x, xg.y - xa.y, Ga.x - Gg.x, Ga.y - Gg.y, u1, u2);
+                ga1 = fma(wa, u1, ga1);
+                ga2 = fma(wa, u2, ga2);
+                a1 = fma(-wg, u1, a1);
+                a2 = fma(-wg, u2, a2);
+                a1 = __shfl_sync(0xffffffffu, a1, (lane + 1) & 31);
+                a2 = __shfl_sync(0xffffffffu, a2, (lane + 1) & 31);
+            }
+            sacc[base + lane] = make_double2(a1, a2);
+            __syncthreads();
+        }
+        double *ap = apart + ((size_t)(k - 1) * nt + J) * 2 * ST;
+        ap[tid] = sacc[tid].x;
+        ap[ST + tid] = sacc[tid].y;
+    }
+    double *gp = gpart + ((size_t)chunk * nt + I) * 2 * ST;
+    gp[tid] = ga1;
+    gp[ST + tid] = ga2;
+}
+
+// FP32 body on head/tail operands: returns the unweighted term u
+__device__ __forceinline__ void pair_u32(const float4 &xg, const float4 &Gg, const float4 &xa,
+                                         const float4 &Ga, float &u1, float &u2) {
+    float d1 = (xg.x - xa.x) + (xg.z - xa.z);
+    float d2 = (xg.y - xa.y) + (xg.w - xa.w);
+    float g1 = (Ga.x - Gg.x) + (Ga.z - Gg.z);
+    float g2 = (Ga.y - Gg.y) + (Ga.w - Gg.w);
+    float r2 = d1 * d1;
+    r2 = fmaf(d2, d2, r2);
+    float y = rsqrtf(r2);
+    y = r2 >= 1e-24f ? y : 0.0f;
+    float dg = d1 * g1;
+    dg = fmaf(d2, g2, dg);
+    float y2 = y * y;
+    float cc = dg * y2;
+    u1 = fmaf(-d1, cc, g1) * y;
+    u2 = fmaf(-d2, cc, g2) * y;
+}
+
+__global__ void __launch_bounds__(ST)
+k_pair32_sym(const float4 *__restrict__ pfx, const float4 *__restrict__ pfg,
+             const float *__restrict__ pfw, int nt, int H, int KC,
+             double *__restrict__ gpart, float *__restrict__ apart) {
+    __shared__ float4 sx[ST], sg[ST];
+    __shared__ float sw[ST];
+    __shared__ float2 sacc[ST];
+    const int I = blockIdx.x % nt, chunk = blockIdx.x / nt;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const float4 xg = pfx[I * ST + tid], Gg = pfg[I * ST + tid];
+    const float wg = pfw[I * ST + tid];
+    double ga1 = 0.0, ga2 = 0.0;
+    const int k0 = chunk * KC, k1 = min(H + 1, k0 + KC);
+    for (int k = k0; k < k1; k++) {
+        if (sym_skip(nt, H, I, k)) continue;
+        const int J = (I + k) % nt;
+        __syncthreads();
+        sx[tid] = pfx[J * ST + tid];
+        sg[tid] = pfg[J * ST + tid];
+        sw[tid] = pfw[J * ST + tid];
+        sacc[tid] = make_float2(0.f, 0.f);
+        __syncthreads();
+        float t1 = 0.f, t2 = 0.f;
+        if (k == 0) {
+#pragma unroll 8
+            for (int a = 0; a < ST; a++) {
+                float u1, u2;
+                pair_u32(xg, Gg, sx[a], sg[a], u1, u2);
+                t1 = fmaf(sw[a], u1, t1);
+                t2 = fmaf(sw[a], u2, t2);
+            }
+            ga1 += (double)t1;
+            ga2 += (double)t2;
+            continue;
+        }
+        for (int r = 0; r < 4; r++) {
+            const int base = ((warp + r) & 3) * 32;
+            float2 a0 = sacc[base + lane];
+            float a1 = a0.x, a2 = a0.y;
+#pragma unroll 8
+            for (int q = 0; q < 32; q++) {
+                const int ai = base + ((lane + q) & 31);
+                float u1, u2;
+                pair_u32(xg, Gg, sx[ai], sg[ai], u1, u2);
+                const float wa = sw[ai];
+                t1 = fmaf(wa, u1, t1);
+                t2 = fmaf(wa, u2, t2);
+                a1 = fmaf(-wg, u1, a1);
+                a2 = fmaf(-wg, u2, a2);
+                a1 = __shfl_sync(0xffffffffu, a1, (lane + 1) & 31);
+                a2 = __shfl_sync(0xffffffffu, a2, (lane + 1) & 31);
+            }
+            sacc[base + lane] = make_float2(a1, a2);
+            __syncthreads();
+        }
+        ga1 += (double)t1;
+        ga2 += (double)t2;
+        float *ap = apart + ((size_t)(k - 1) * nt + J) * 2 * ST;
+        ap[tid] = sacc[tid].x;
+        ap[ST + tid] = sacc[tid].y;
+    }
+    double *gp = gpart + ((size_t)chunk * nt + I) * 2 * ST;
+    gp[tid] = ga1;
+    gp[ST + tid] = ga2;
+}
+
+// vdot[p] = sum over chunks of the target-side partials + sum over k of the
+// source-side partials, in that fixed order
+template <typename TA>
+__global__ void k_sym_reduce(const double *__restrict__ gpart, const TA *__restrict__ apart,
+                             int nt, int H, int nchunk, double *__restrict__ dst, size_t ld) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nt * ST) return;
+    int K = p / ST, t = p - K * ST;
+    double s1 = 0.0, s2 = 0.0;
+    for (int c = 0; c < nchunk; c++) {
+        const double *gp = gpart + ((size_t)c * nt + K) * 2 * ST;
+        s1 += gp[t];
+        s2 += gp[ST + t];
+    }
+    for (int k = 1; k <= H; k++) {
+        int I = (K - k + nt) % nt;
+        if (sym_skip(nt, H, I, k)) continue;
+        const TA *ap = apart + ((size_t)(k - 1) * nt + K) * 2 * ST;
+        s1 += (double)ap[t];
+        s2 += (double)ap[ST + t];
+    }
+    dst[p] = s1;
+    dst[ld + p] = s2;
+}
+
 // sum the slice partials of components [c0, c0+nc) in slice order into
 // dst (nc x ld); the partials hold ncomp components per slice
 __global__ void k_slice_reduce(const double *__restrict__ part, int split, int ncomp, int c0,
@@ -251,7 +534,7 @@ __global__ void k_slice_reduce(const double *__restrict__ part, int split, int n
 
 // Landau pack: lambda from the device state, G_eff = -(dS + lambda dv)/w
 // (solver.jl:107-111), operands in sorted order.
-__global__ void k_pack_landau(const int *__restrict__ perm, const int *__restrict__ Mp, int N,
+__global__ void k_pack_landau(const int *__restrict__ perm, const int *__restrict__ Mp, int Mpad, int N,
                               const double *__restrict__ vmid, const double *__restrict__ dS,
                               const double *__restrict__ dv, const double *__restrict__ w,
                               const co_solver_state *__restrict__ st, int use_lambda,
@@ -260,19 +543,33 @@ __global__ void k_pack_landau(const int *__restrict__ perm, const int *__restric
                               float4 *__restrict__ pfg, float *__restrict__ pfw) {
     int M = *Mp;
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= M) return;
+    if (p >= Mpad) return;
+    if (p >= M) {  // inert padding up to the tile boundary: far away, zero weight
+        if (precision != CO_PREC_FP64) {
+            pfx[p] = make_float4(1e3f, 1e3f, 0.f, 0.f);
+            pfg[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+            pfw[p] = 0.f;
+        }
+        if (precision != CO_PREC_MIXED) {
+            px[p] = make_double2(1e3, 1e3);
+            pg[p] = make_double2(0.0, 0.0);
+            pw[p] = 0.0;
+        }
+        return;
+    }
     int a = perm[p];
     double lam = use_lambda ? st->lambda : 0.0;
     double iw = 1.0 / w[a];
     double x1 = vmid[a], x2 = vmid[N + a];
     double G1 = -(dS[a] + lam * dv[a]) * iw;
     double G2 = -(dS[N + a] + lam * dv[N + a]) * iw;
-    if (precision == CO_PREC_MIXED) {
+    if (precision != CO_PREC_FP64) {
         float x1h = (float)x1, x2h = (float)x2, G1h = (float)G1, G2h = (float)G2;
         pfx[p] = make_float4(x1h, x2h, (float)(x1 - (double)x1h), (float)(x2 - (double)x2h));
         pfg[p] = make_float4(G1h, G2h, (float)(G1 - (double)G1h), (float)(G2 - (double)G2h));
         pfw[p] = (float)w[a];
-    } else {
+    }
+    if (precision != CO_PREC_MIXED) {
         px[p] = make_double2(x1, x2);
         pg[p] = make_double2(G1, G2);
         pw[p] = w[a];
@@ -280,7 +577,7 @@ __global__ void k_pack_landau(const int *__restrict__ perm, const int *__restric
 }
 
 // Hook pack: operands straight from (v, G, w) (COLLISION_FN semantics).
-__global__ void k_pack_plain(const int *__restrict__ perm, const int *__restrict__ Mp, int N,
+__global__ void k_pack_plain(const int *__restrict__ perm, const int *__restrict__ Mp, int Mpad, int N,
                              const double *__restrict__ v, const double *__restrict__ G,
                              const double *__restrict__ w, int precision,
                              double2 *__restrict__ px, double2 *__restrict__ pg,
@@ -288,15 +585,29 @@ __global__ void k_pack_plain(const int *__restrict__ perm, const int *__restrict
                              float4 *__restrict__ pfg, float *__restrict__ pfw) {
     int M = *Mp;
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= M) return;
+    if (p >= Mpad) return;
+    if (p >= M) {  // inert padding up to the tile boundary: far away, zero weight
+        if (precision != CO_PREC_FP64) {
+            pfx[p] = make_float4(1e3f, 1e3f, 0.f, 0.f);
+            pfg[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+            pfw[p] = 0.f;
+        }
+        if (precision != CO_PREC_MIXED) {
+            px[p] = make_double2(1e3, 1e3);
+            pg[p] = make_double2(0.0, 0.0);
+            pw[p] = 0.0;
+        }
+        return;
+    }
     int a = perm[p];
     double x1 = v[a], x2 = v[N + a], G1 = G[a], G2 = G[N + a];
-    if (precision == CO_PREC_MIXED) {
+    if (precision != CO_PREC_FP64) {
         float x1h = (float)x1, x2h = (float)x2, G1h = (float)G1, G2h = (float)G2;
         pfx[p] = make_float4(x1h, x2h, (float)(x1 - (double)x1h), (float)(x2 - (double)x2h));
         pfg[p] = make_float4(G1h, G2h, (float)(G1 - (double)G1h), (float)(G2 - (double)G2h));
         pfw[p] = (float)w[a];
-    } else {
+    }
+    if (precision != CO_PREC_MIXED) {
         px[p] = make_double2(x1, x2);
         pg[p] = make_double2(G1, G2);
         pw[p] = w[a];
@@ -381,8 +692,11 @@ static int ensure_part(co_ctx *c, size_t n) {
 }
 
 // M is an upper bound (N); the true count sits at cstart[n_el] on the device.
+static int pair_sym(co_ctx *c, int Mub, int fp64);
+
 int co_pair_fp64(co_ctx *c, int Mub, int with_metric) {
     if (Mub <= 0) return CO_OK;
+    if (!with_metric && c->pair_symmetric && co_cdiv(Mub, ST) >= 4) return pair_sym(c, Mub, 1);
     const int *Mp = c->mb.cstart + c->n_el;
     size_t ld = (size_t)c->mb.cap;
     int split = choose_split(c, Mub, PAIR_TPB, c->pair_split_fp64);
@@ -397,12 +711,14 @@ int co_pair_fp64(co_ctx *c, int Mub, int with_metric) {
         if (rc) return rc;
         dst = c->mb.part;
     }
+    co_prof_begin(c, 1);
     if (with_metric)
         k_pair64<true><<<grid, PAIR_TPB, 0, c->stream>>>(c->mb.px, c->mb.pg, c->mb.pw, Mp, slice,
                                                          dst, ld);
     else
         k_pair64<false><<<grid, PAIR_TPB, 0, c->stream>>>(c->mb.px, c->mb.pg, c->mb.pw, Mp, slice,
                                                           dst, ld);
+    co_prof_end(c);
     c->launches++;
     if (with_metric) {
         // components 0,1 -> pdot ; 2,3,4 -> pA
@@ -420,7 +736,44 @@ int co_pair_fp64(co_ctx *c, int Mub, int with_metric) {
     return CO_OK;
 }
 
+#define SYM_KC 8
+
+// symmetric pair sum on the padded operands (Mpad = nt * ST)
+static int pair_sym(co_ctx *c, int Mub, int fp64) {
+    int nt = co_cdiv(Mub, ST);
+    int H = nt / 2;
+    int KC = SYM_KC;
+    int nchunk = co_cdiv(H + 1, KC);
+    size_t gsz = (size_t)nchunk * nt * 2 * ST;               // doubles
+    size_t asz = (size_t)(H > 0 ? H : 1) * nt * 2 * ST;      // doubles (fp64) / floats (fp32)
+    size_t need = gsz + (fp64 ? asz : (asz + 1) / 2);
+    int rc = ensure_part(c, need);
+    if (rc) return rc;
+    double *gpart = c->mb.part;
+    co_prof_begin(c, fp64);
+    if (fp64) {
+        double *apart = c->mb.part + gsz;
+        k_pair64_sym<<<nt * nchunk, ST, 0, c->stream>>>(c->mb.px, c->mb.pg, c->mb.pw, nt, H, KC,
+                                                        gpart, apart);
+        co_prof_end(c);
+        k_sym_reduce<double><<<co_cdiv((long long)nt * ST, 256), 256, 0, c->stream>>>(
+            gpart, apart, nt, H, nchunk, c->mb.pdot, (size_t)c->mb.cap);
+    } else {
+        float *apart = (float *)(c->mb.part + gsz);
+        k_pair32_sym<<<nt * nchunk, ST, 0, c->stream>>>(c->mb.pf_x, c->mb.pf_g, c->mb.pf_w, nt, H,
+                                                        KC, gpart, apart);
+        co_prof_end(c);
+        k_sym_reduce<float><<<co_cdiv((long long)nt * ST, 256), 256, 0, c->stream>>>(
+            gpart, apart, nt, H, nchunk, c->mb.pdot, (size_t)c->mb.cap);
+    }
+    c->launches += 2;
+    CO_CK(cudaGetLastError());
+    return CO_OK;
+}
+
 int co_pair_fp32(co_ctx *c, int Mub) {
+    if (Mub <= 0) return CO_OK;
+    if (c->pair_symmetric && co_cdiv(Mub, ST) >= 4) return pair_sym(c, Mub, 0);
     if (Mub <= 0) return CO_OK;
     const int *Mp = c->mb.cstart + c->n_el;
     size_t ld = (size_t)c->mb.cap;
@@ -435,8 +788,10 @@ int co_pair_fp32(co_ctx *c, int Mub) {
         if (rc) return rc;
         dst = c->mb.part;
     }
+    co_prof_begin(c, 0);
     k_pair32<<<grid, PAIR_TPB, 0, c->stream>>>(c->mb.pf_x, c->mb.pf_g, c->mb.pf_w, Mp, slice, dst,
                                                ld);
+    co_prof_end(c);
     c->launches++;
     if (split > 1) {
         k_slice_reduce<<<co_cdiv(Mub, 256), 256, 0, c->stream>>>(dst, split, 2, 0, 2, ld, Mp,
@@ -451,7 +806,8 @@ int co_pack_plain(co_ctx *c, int N, int Mub, int precision, const double *x, con
     if (Mub <= 0) return CO_OK;
     const int *Mp = c->mb.cstart + c->n_el;
     co_bufs &b = c->mb;
-    k_pack_plain<<<co_cdiv(Mub, 256), 256, 0, c->stream>>>(b.perm, Mp, N, x, G, b.w, precision,
+    int Mpad = co_cdiv(Mub, PAIR_TPB) * PAIR_TPB;
+    k_pack_plain<<<co_cdiv(Mpad, 256), 256, 0, c->stream>>>(b.perm, Mp, Mpad, N, x, G, b.w, precision,
                                                            b.px, b.pg, b.pw, b.pf_x, b.pf_g,
                                                            b.pf_w);
     c->launches++;
@@ -463,8 +819,9 @@ int co_pack_landau(co_ctx *c, int N, int Mub, int precision, int gonzalez) {
     if (Mub <= 0) return CO_OK;
     const int *Mp = c->mb.cstart + c->n_el;
     co_bufs &b = c->mb;
-    k_pack_landau<<<co_cdiv(Mub, 256), 256, 0, c->stream>>>(
-        b.perm, Mp, N, b.vmid, b.dS, b.dv, b.w, c->st, gonzalez, precision, b.px, b.pg, b.pw,
+    int Mpad = co_cdiv(Mub, PAIR_TPB) * PAIR_TPB;
+    k_pack_landau<<<co_cdiv(Mpad, 256), 256, 0, c->stream>>>(
+        b.perm, Mp, Mpad, N, b.vmid, b.dS, b.dv, b.w, c->st, gonzalez, precision, b.px, b.pg, b.pw,
         b.pf_x, b.pf_g, b.pf_w);
     c->launches++;
     CO_CK(cudaGetLastError());
@@ -488,6 +845,16 @@ int co_unpack_A(co_ctx *c, int N, double *A) {
     if (N == 0) return CO_OK;
     k_unpack_A<<<co_cdiv(N, 256), 256, 0, c->stream>>>(c->mb.inv, N, c->mb.pA, (size_t)c->mb.cap,
                                                        A);
+    c->launches++;
+    CO_CK(cudaGetLastError());
+    return CO_OK;
+}
+
+int co_metric32(co_ctx *c, int Mub) {
+    if (Mub <= 0) return CO_OK;
+    const int *Mp = c->mb.cstart + c->n_el;
+    k_metric32<<<co_cdiv(Mub, PAIR_TPB), PAIR_TPB, 0, c->stream>>>(c->mb.pf_x, c->mb.pf_w, Mp,
+                                                                   c->mb.pA, (size_t)c->mb.cap);
     c->launches++;
     CO_CK(cudaGetLastError());
     return CO_OK;

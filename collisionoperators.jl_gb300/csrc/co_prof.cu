@@ -1,0 +1,183 @@
+// co_prof.cu -- measurement support: CUDA-event timing of the pair kernels on
+// the context's stream, and an FMA-chain probe of the GPU's FP32/FP64 peak.
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "co_internal.cuh"
+
+#define CO_PROF_POOL 8192
+
+struct co_prof_pair {
+    cudaEvent_t a, b;
+    int fp64;
+    int slot;  // index into the pinned M array
+};
+
+struct co_prof {
+    int on;
+    std::vector<cudaEvent_t> pool;  // 2 * CO_PROF_POOL events
+    std::vector<co_prof_pair> pending;
+    int *Mpinned;                   // in-domain count of each pending launch
+    co_profile_t acc;
+};
+
+static co_prof *get_prof(co_ctx *c) {
+    if (!c->prof) {
+        co_prof *p = new co_prof();
+        p->on = 0;
+        p->Mpinned = nullptr;
+        memset(&p->acc, 0, sizeof(p->acc));
+        c->prof = p;
+    }
+    return c->prof;
+}
+
+void co_prof_collect(co_ctx *c) {
+    co_prof *p = c->prof;
+    if (!p || p->pending.empty()) return;
+    for (auto &e : p->pending) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, e.a, e.b) != cudaSuccess) continue;
+        double M = (double)p->Mpinned[e.slot];
+        if (e.fp64) {
+            p->acc.pair64_ms += ms;
+            p->acc.pair64_launches++;
+            p->acc.pair64_pairs += M * (M - 1.0);
+        } else {
+            p->acc.pair32_ms += ms;
+            p->acc.pair32_launches++;
+            p->acc.pair32_pairs += M * (M - 1.0);
+        }
+    }
+    p->pending.clear();
+}
+
+void co_prof_begin(co_ctx *c, int fp64) {
+    co_prof *p = c->prof;
+    if (!p || !p->on) return;
+    if ((int)p->pending.size() >= CO_PROF_POOL) {
+        cudaStreamSynchronize(c->stream);
+        co_prof_collect(c);
+    }
+    int i = (int)p->pending.size();
+    co_prof_pair e;
+    e.a = p->pool[2 * i];
+    e.b = p->pool[2 * i + 1];
+    e.fp64 = fp64;
+    e.slot = i;
+    p->pending.push_back(e);
+    cudaEventRecord(e.a, c->stream);
+}
+
+void co_prof_end(co_ctx *c) {
+    co_prof *p = c->prof;
+    if (!p || !p->on || p->pending.empty()) return;
+    co_prof_pair &e = p->pending.back();
+    cudaEventRecord(e.b, c->stream);
+    cudaMemcpyAsync(&p->Mpinned[e.slot], c->mb.cstart + c->n_el, sizeof(int),
+                    cudaMemcpyDeviceToHost, c->stream);
+}
+
+void co_prof_free(co_ctx *c) {
+    co_prof *p = c->prof;
+    if (!p) return;
+    for (cudaEvent_t e : p->pool) cudaEventDestroy(e);
+    if (p->Mpinned) cudaFreeHost(p->Mpinned);
+    delete p;
+    c->prof = nullptr;
+}
+
+extern "C" int co_profile(co_ctx *c, int enable) {
+    if (!c) return CO_ERR_ARG;
+    CO_CK(cudaSetDevice(c->device));
+    co_prof *p = get_prof(c);
+    CO_CK(cudaStreamSynchronize(c->stream));
+    co_prof_collect(c);
+    if (enable) {
+        if (p->pool.empty()) {
+            p->pool.resize(2 * CO_PROF_POOL);
+            for (auto &e : p->pool) CO_CK(cudaEventCreate(&e));
+            CO_CK(cudaMallocHost(&p->Mpinned, sizeof(int) * CO_PROF_POOL));
+        }
+        memset(&p->acc, 0, sizeof(p->acc));
+        c->maps32 = c->maps64 = 0;
+    }
+    p->on = enable ? 1 : 0;
+    return CO_OK;
+}
+
+extern "C" int co_profile_read(co_ctx *c, co_profile_t *out) {
+    if (!c || !out) return CO_ERR_ARG;
+    CO_CK(cudaSetDevice(c->device));
+    co_prof *p = get_prof(c);
+    CO_CK(cudaStreamSynchronize(c->stream));
+    co_prof_collect(c);
+    *out = p->acc;
+    out->maps64 = c->maps64;
+    out->maps32 = c->maps32;
+    return CO_OK;
+}
+
+extern "C" int co_ctx_stream(const co_ctx *c, void **stream) {
+    if (!c || !stream) return CO_ERR_ARG;
+    *stream = (void *)c->stream;
+    return CO_OK;
+}
+
+// ---------------------------------------------------------------- peak probe
+
+#define PEAK_CHAINS 8
+#define PEAK_ITERS 4096
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_fma_chain(T *out, T a, T b) {
+    T x[PEAK_CHAINS];
+#pragma unroll
+    for (int k = 0; k < PEAK_CHAINS; k++) x[k] = (T)(threadIdx.x + k);
+    for (int it = 0; it < PEAK_ITERS; it++) {
+#pragma unroll
+        for (int k = 0; k < PEAK_CHAINS; k++) x[k] = x[k] * a + b;
+    }
+    T s = 0;
+#pragma unroll
+    for (int k = 0; k < PEAK_CHAINS; k++) s += x[k];
+    if (s == (T)1.2345e-7) out[0] = s;  // keeps the chains live
+}
+
+extern "C" int co_measure_fma_peak(int device, int fp64, double *flops) {
+    if (!flops) return CO_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return CO_ERR_NODEVICE;
+    if (device < 0 || device >= ndev) return CO_ERR_ARG;
+    CO_CK(cudaSetDevice(device));
+    cudaDeviceProp prop;
+    CO_CK(cudaGetDeviceProperties(&prop, device));
+    int blocks = prop.multiProcessorCount * (fp64 ? 4 : 8);
+    void *out = nullptr;
+    CO_CK(cudaMalloc(&out, 16));
+    cudaEvent_t e0, e1;
+    CO_CK(cudaEventCreate(&e0));
+    CO_CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int reps = fp64 ? 2 : 3;
+    for (int r = 0; r < reps + 1; r++) {
+        CO_CK(cudaEventRecord(e0));
+        if (fp64)
+            k_fma_chain<double><<<blocks, 256>>>((double *)out, 0.999999, 1e-7);
+        else
+            k_fma_chain<float><<<blocks, 256>>>((float *)out, 0.999999f, 1e-7f);
+        CO_CK(cudaEventRecord(e1));
+        CO_CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CO_CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (r > 0 && ms < best) best = ms;  // first launch is warm-up
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    double fl = 2.0 * PEAK_CHAINS * (double)PEAK_ITERS * 256.0 * blocks;
+    *flops = fl / (best * 1e-3);
+    return CO_OK;
+}

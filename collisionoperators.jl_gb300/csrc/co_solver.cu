@@ -121,6 +121,7 @@ k_lb_fused(int N, const double *__restrict__ vmid, const double *__restrict__ w,
         if (threadIdx.x == 0) red7[blockIdx.x * 8 + k] = s;
     }
     grid_barrier(bar, gridDim.x, err);
+    if (threadIdx.x == 0 && *((volatile int *)err)) st->error = CO_ERR_TIMEOUT;
     // every block reduces the partials in the same fixed order
     double tot[7];
     for (int k = 0; k < 7; k++) tot[k] = co_sum_partials(red7, gridDim.x, 8, k, sh);
@@ -176,6 +177,7 @@ __global__ void k_state_reset(co_solver_state *st) {
         st->history = 0;
         st->slot = 0;
         st->n_restart = 0;
+        st->k64 = 0;
         st->done = 0;
         st->path = 0;
         st->improved = 0;
@@ -197,6 +199,10 @@ k_ctrl1(const double *__restrict__ red, int nred, co_solver_state *st, co_dev_op
     double r2 = co_sum_partials(red, nred, 2, 0, sh);
     double v2 = co_sum_partials(red, nred, 2, 1, sh);
     if (threadIdx.x != 0) return;
+    if (st->error) {
+        st->done = 4;
+        return;
+    }
     int k = st->k + 1;
     st->k = k;
     double nrm_r = sqrt(r2), nrm_v = sqrt(v2);
@@ -445,6 +451,33 @@ int co_lb_fused(co_ctx *c, int N, double nu, double dt, double *Gv, const double
     return CO_OK;
 }
 
+// landau_geff! (solver.jl:86-113) after the v_mid projection: r, L = M^{-1} r,
+// grad L at v_mid with dS = -w G and the Gonzalez partials, then lambda.
+static int landau_tail(co_ctx *c, int gonzalez, int N, double S0, int nred) {
+    int rc;
+    co_bufs &b = c->mb;
+    if ((rc = co_compute_r_dev(c, c->f, c->rr))) return rc;
+    if ((rc = co_mass_solve_dev(c, c->rr, c->L))) return rc;
+    if ((rc = co_grad_L_dev(c, b.vmid, N, c->L, b.G, b.w, b.dS, b.dv, b.red))) return rc;
+    k_lambda<<<1, 256, 0, c->stream>>>(b.red, nred, c->st, S0, gonzalez);
+    c->launches++;
+    CO_CK(cudaGetLastError());
+    return CO_OK;
+}
+
+// full landau_geff! at v_in: leaves dS, dv, lambda (st) and the sorted v_mid
+static int landau_geff_dev(co_ctx *c, int gonzalez, const double *vin, const double *v0, int N,
+                           double S0) {
+    int rc;
+    co_bufs &b = c->mb;
+    if (gonzalez)
+        if ((rc = entropy_into_state(c, vin, N))) return rc;
+    if ((rc = co_mid_dv(c, vin, v0, N))) return rc;
+    if ((rc = co_sort_markers(c, b.vmid, N))) return rc;
+    if ((rc = co_project_sorted(c, c->f))) return rc;
+    return landau_tail(c, gonzalez, N, S0, red_blocks(c, N));
+}
+
 // One Picard map on device buffers. vin/v0/w device pointers (w must be
 // c->mb.w). If r != nullptr, r = Gv - vin with residual partials in mb.red.
 static int picard_map_impl(co_ctx *c, int model, int gonzalez, double nu, int precision,
@@ -474,17 +507,15 @@ static int picard_map_impl(co_ctx *c, int model, int gonzalez, double nu, int pr
         if (grid < 1) grid = 1;
         nred = grid;
     } else {
-        if ((rc = co_compute_r_dev(c, c->f, c->rr))) return rc;
-        if ((rc = co_mass_solve_dev(c, c->rr, c->L))) return rc;
-        if ((rc = co_grad_L_dev(c, b.vmid, N, c->L, b.G, b.w, b.dS, b.dv, b.red))) return rc;
-        k_lambda<<<1, 256, 0, c->stream>>>(b.red, nred, c->st, S0, gonzalez);
-        c->launches++;
-        CO_CK(cudaGetLastError());
+        if ((rc = landau_tail(c, gonzalez, N, S0, nred))) return rc;
         if ((rc = co_pack_landau(c, N, N, precision, gonzalez))) return rc;
-        if (precision == CO_PREC_MIXED)
+        if (precision == CO_PREC_MIXED) {
             rc = co_pair_fp32(c, N);
-        else
+            c->maps32++;
+        } else {
             rc = co_pair_fp64(c, N, 0);
+            c->maps64++;
+        }
         if (rc) return rc;
         if ((rc = co_unpack_update(c, N, dt, Gv, v0, vin, r, r ? b.red : nullptr))) return rc;
     }
@@ -551,6 +582,7 @@ static int anderson_loop(co_ctx *c, const co_opts *o, int precision, int N, doub
         CO_CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(co_solver_state), cudaMemcpyDeviceToHost,
                               c->stream));
         CO_CK(cudaStreamSynchronize(c->stream));
+        co_prof_collect(c);
         if (c->st_host->done) break;
     }
     if (k > max_iter) {
@@ -646,5 +678,297 @@ int co_predictor_buffers(co_ctx *c, const co_opts *o, int precision, const doubl
         if ((rc = co_unpack_update(c, N, dt, out, v, nullptr, nullptr, nullptr))) return rc;
     }
     CO_CK(cudaGetLastError());
+    return CO_OK;
+}
+
+// ================================================================ defect correction
+//
+// step_defect! (solver.jl:569-634) with _anderson_inner! (solver.jl:492-526).
+// Outer iteration k: G_eff(v_k) and the full Picard map G(v_k) with the pair
+// sum -- FP64 in the plain form; in the mixed form FP32 until the FP32 outer
+// residual stalls, then FP64 -- plus the frozen metric A_k (FP32 kernel, it only
+// shapes the inner model). Inner: Anderson on
+//     Phi_k(u) = G(v_k) - dt A_k (G_eff(u) - G_eff(v_k))
+// to max(eta ||G(v_k) - v_k||, abs_floor/2); each Phi_k needs the O(N)
+// projection chain but no pair sum. The exit returns G(v) from a pair sum, so
+// momentum and energy are conserved as in step_anderson!.
+
+// G_eff = -(dS + lambda dv)/w in marker order (solver.jl:107-111)
+__global__ void k_geff_store(int N, const double *__restrict__ dS, const double *__restrict__ dv,
+                             const double *__restrict__ w, const co_solver_state *st, int use_lambda,
+                             double *__restrict__ Gk) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= N) return;
+    double lam = use_lambda ? st->lambda : 0.0;
+    double iw = 1.0 / w[a];
+    Gk[a] = -(dS[a] + lam * dv[a]) * iw;
+    Gk[N + a] = -(dS[N + a] + lam * dv[N + a]) * iw;
+}
+
+// frozen_map! (solver.jl:585-595): Phi = Gv - dt A (G_eff(u) - Gk), r = Phi - u
+__global__ void __launch_bounds__(CO_RED_THREADS)
+k_frozen_map(int N, const double *__restrict__ Gv, const double *__restrict__ A,
+             const double *__restrict__ Gk, const double *__restrict__ dS,
+             const double *__restrict__ dv, const double *__restrict__ w,
+             const co_solver_state *st, int use_lambda, double dt, const double *__restrict__ u,
+             double *__restrict__ Phi, double *__restrict__ r, double *__restrict__ red) {
+    __shared__ double sh[32];
+    double lam = use_lambda ? st->lambda : 0.0;
+    double sr = 0.0;
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < N; a += gridDim.x * blockDim.x) {
+        double iw = 1.0 / w[a];
+        double d1 = -(dS[a] + lam * dv[a]) * iw - Gk[a];
+        double d2 = -(dS[N + a] + lam * dv[N + a]) * iw - Gk[N + a];
+        double A11 = A[a], A12 = A[N + a], A22 = A[2 * (size_t)N + a];
+        double p1 = Gv[a] - dt * (A11 * d1 + A12 * d2);
+        double p2 = Gv[N + a] - dt * (A12 * d1 + A22 * d2);
+        Phi[a] = p1;
+        Phi[N + a] = p2;
+        double r1 = p1 - u[a], r2 = p2 - u[N + a];
+        r[a] = r1;
+        r[N + a] = r2;
+        sr += r1 * r1 + r2 * r2;
+    }
+    double s = co_block_sum(sr, sh);
+    if (threadIdx.x == 0) {
+        red[blockIdx.x * 2 + 0] = s;
+        red[blockIdx.x * 2 + 1] = 0.0;
+    }
+}
+
+struct co_defect_dev {
+    double tol, abs_floor, eta, stag_rel_tol, fp32_stall;
+    int stag_window;
+};
+
+// outer decisions (solver.jl:603-626). stage: 1 = FP32 outer map, 0 = FP64.
+// st->path <- next stage; st->res_out <- inner tolerance.
+__global__ void __launch_bounds__(256)
+k_ctrl_outer(const double *__restrict__ red, int nred, co_solver_state *st, co_defect_dev o,
+             int stage) {
+    __shared__ double sh[32];
+    if (st->done) return;
+    double r2 = co_sum_partials(red, nred, 2, 0, sh);
+    double v2 = co_sum_partials(red, nred, 2, 1, sh);
+    if (threadIdx.x != 0) return;
+    if (st->error) {
+        st->done = 4;
+        return;
+    }
+    int k = st->k + 1;
+    st->k = k;
+    double nrm = sqrt(r2), nv = sqrt(v2);
+    st->nrm_v = nv;
+    if (!isfinite(nrm)) {
+        st->error = CO_ERR_NONFINITE;
+        st->done = 4;
+        return;
+    }
+    st->improved = 0;
+    if (stage == 1) {
+        // FP32 outer maps: stop them once the residual no longer halves
+        // (the FP32 noise floor); the FP64 stage then takes over
+        double prev = st->nrm_r;
+        st->nrm_r = nrm;
+        if (k == 1) st->nrm_r0 = nrm;
+        if ((k > 1 && nrm > o.fp32_stall * prev) || nrm < fmax(o.tol * (nv + 1e-30), o.abs_floor))
+            st->path = 0;
+        else
+            st->path = 1;
+        st->res_out = fmax(o.eta * nrm, 0.5 * o.abs_floor);
+        return;
+    }
+    st->nrm_r = nrm;
+    if (st->k64 == 0) {  // first FP64 outer map: the stopping rule starts here
+        st->nrm_best = INFINITY;
+        st->nrm_best_window = INFINITY;
+        if (k == 1) st->nrm_r0 = nrm;
+    }
+    st->k64 += 1;
+    int k64 = st->k64;
+    if (nrm < st->nrm_best) {
+        st->nrm_best = nrm;
+        st->improved = 1;
+    }
+    if (nrm < fmax(o.tol * (nv + 1e-30), o.abs_floor)) {
+        st->done = 1;
+        st->res_out = nrm;
+        return;
+    }
+    if (k64 > o.stag_window && k64 % o.stag_window == 0) {
+        if ((st->nrm_best_window - st->nrm_best) / (st->nrm_best_window + 1e-30) < o.stag_rel_tol) {
+            st->done = 2;
+            st->res_out = st->nrm_best;
+            return;
+        }
+        st->nrm_best_window = st->nrm_best;
+    }
+    st->path = 0;
+    st->res_out = fmax(o.eta * nrm, 0.5 * o.abs_floor);
+}
+
+// vbest <- Gv when the outer residual improved
+__global__ void k_defect_best(int n2, const co_solver_state *st, const double *__restrict__ Gv,
+                              double *__restrict__ vbest) {
+    if (!st->improved) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x)
+        vbest[i] = Gv[i];
+}
+
+// inner Anderson control (solver.jl:497-521): tolerance from the outer state
+__global__ void __launch_bounds__(256)
+k_ctrl_inner(const double *__restrict__ red, int nred, co_solver_state *si,
+             const co_solver_state *so, int m, double damping) {
+    __shared__ double sh[32];
+    if (si->done) return;
+    double r2 = co_sum_partials(red, nred, 2, 0, sh);
+    if (threadIdx.x != 0) return;
+    int k = si->k + 1;
+    si->k = k;
+    double nrm = sqrt(r2);
+    si->nrm_r = nrm;
+    si->improved = 0;
+    if (!isfinite(nrm)) {
+        si->error = CO_ERR_NONFINITE;
+        si->done = 4;
+        return;
+    }
+    if (nrm < so->res_out) {
+        si->done = 1;
+        return;
+    }
+    si->damp = damping;
+    if (k == 1) {
+        si->path = 0;
+    } else {
+        si->path = 1;
+        si->slot = si->slot % m + 1;
+        si->history = si->history + 1 < m ? si->history + 1 : m;
+    }
+}
+
+__global__ void k_copy_if_done(int n2, const co_solver_state *st, int want, double *__restrict__ dst,
+                               const double *__restrict__ src) {
+    if (st->done != want) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
+int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *dopt, int N,
+                           double S0, double dt, int *outer, double *res, int *inner,
+                           double *r0) {
+    int rc;
+    if (o->m < 1 || o->m > CO_MAX_M) return CO_ERR_ARG;
+    if ((rc = co_ensure_capacity(c, N, o->m))) return rc;
+    if (N == 0) {
+        if (outer) *outer = 0;
+        if (res) *res = 0;
+        if (inner) *inner = 0;
+        if (r0) *r0 = 0;
+        return CO_OK;
+    }
+    if (!c->st2 && cudaMalloc(&c->st2, sizeof(co_solver_state)) != cudaSuccess) return CO_ERR_NOMEM;
+    co_bufs &b = c->mb;
+    if (!b.Gk && cudaMalloc(&b.Gk, 2 * sizeof(double) * b.cap) != cudaSuccess) return CO_ERR_NOMEM;
+    if (!b.Phi && cudaMalloc(&b.Phi, 2 * sizeof(double) * b.cap) != cudaSuccess) return CO_ERR_NOMEM;
+    if (!b.Adef && cudaMalloc(&b.Adef, 3 * sizeof(double) * b.cap) != cudaSuccess) return CO_ERR_NOMEM;
+    const int n2 = 2 * N;
+    const size_t ldF = 2 * (size_t)b.cap;
+    const int eg = ew_grid(c, n2);
+    const int nred = red_blocks(c, N);
+    const int gz = o->use_gonzalez;
+    co_defect_dev d;
+    d.tol = o->tol;
+    d.abs_floor = o->abs_floor;
+    d.eta = dopt->eta;
+    d.stag_rel_tol = o->stag_rel_tol;
+    d.stag_window = dopt->stag_window;
+    d.fp32_stall = dopt->fp32_stall > 0 ? dopt->fp32_stall : 0.5;
+    co_dev_opts di = dev_opts(o, 0.0);
+    int stage = o->precision == CO_PREC_MIXED ? 1 : 0;
+    int max_outer = o->max_iter;
+    int total_inner = 0;
+    k_state_reset<<<1, 32, 0, c->stream>>>(c->st);
+    c->launches++;
+    int k;
+    for (k = 1; k <= max_outer; k++) {
+        // ---- outer: G_eff(v_k), F (+ A), G(v_k), residual
+        if ((rc = landau_geff_dev(c, gz, b.v1, b.v0, N, S0))) return rc;
+        k_geff_store<<<co_cdiv(N, 256), 256, 0, c->stream>>>(N, b.dS, b.dv, b.w, c->st, gz, b.Gk);
+        c->launches++;
+        const int m64 = dopt->metric64 && stage == 0;
+        int prec_pack = stage == 1 ? CO_PREC_MIXED : (m64 ? CO_PREC_FP64 : CO_PREC_BOTH);
+        if ((rc = co_pack_landau(c, N, N, prec_pack, gz))) return rc;
+        if (stage == 1) {
+            rc = co_pair_fp32(c, N);
+            c->maps32++;
+        } else {
+            rc = co_pair_fp64(c, N, m64);   // with_metric: F and A in one FP64 pass
+            c->maps64++;
+        }
+        if (rc) return rc;
+        if ((rc = co_unpack_update(c, N, dt, b.Gv, b.v0, b.v1, b.r, b.red))) return rc;
+        if (!m64)
+            if ((rc = co_metric32(c, N))) return rc;
+        if ((rc = co_unpack_A(c, N, b.Adef))) return rc;
+        k_ctrl_outer<<<1, 256, 0, c->stream>>>(b.red, nred, c->st, d, stage);
+        k_defect_best<<<eg, 256, 0, c->stream>>>(n2, c->st, b.Gv, b.vbest);
+        c->launches += 2;
+        CO_CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(co_solver_state), cudaMemcpyDeviceToHost,
+                              c->stream));
+        CO_CK(cudaStreamSynchronize(c->stream));
+        co_prof_collect(c);
+        if (c->st_host->error) return c->st_host->error;
+        if (c->st_host->done) break;
+        int next_stage = stage == 1 ? c->st_host->path : 0;
+        // ---- inner: Anderson on the frozen-metric map (u = v1 in place)
+        k_state_reset<<<1, 32, 0, c->stream>>>(c->st2);
+        c->launches++;
+        int j;
+        for (j = 1; j <= dopt->max_inner; j++) {
+            if ((rc = landau_geff_dev(c, gz, b.v1, b.v0, N, S0))) return rc;
+            k_frozen_map<<<nred, CO_RED_THREADS, 0, c->stream>>>(N, b.Gv, b.Adef, b.Gk, b.dS, b.dv,
+                                                               b.w, c->st, gz, dt, b.v1, b.Phi, b.r,
+                                                               b.red);
+            k_ctrl_inner<<<1, 256, 0, c->stream>>>(b.red, nred, c->st2, c->st, o->m, o->damping);
+            k_plain_update<<<eg, 256, 0, c->stream>>>(n2, c->st2, 0, b.v1, b.Phi, b.r, b.rp, b.Gp,
+                                                      b.vbest);
+            int ng = red_blocks(c, n2);
+            k_anderson_cols<<<ng, CO_RED_THREADS, 0, c->stream>>>(n2, c->st2, b.r, b.rp, b.Phi,
+                                                                  b.Gp, b.dF, b.dG, ldF, b.red);
+            k_anderson_solve<<<1, 256, 0, c->stream>>>(b.red, ng, c->st2, di);
+            k_anderson_update<<<eg, 256, 0, c->stream>>>(n2, c->st2, b.v1, b.Phi, b.dG, ldF);
+            c->launches += 6;
+            CO_CK(cudaGetLastError());
+            CO_CK(cudaMemcpyAsync(c->st_host, c->st2, sizeof(co_solver_state),
+                                  cudaMemcpyDeviceToHost, c->stream));
+            CO_CK(cudaStreamSynchronize(c->stream));
+            if (c->st_host->error) return c->st_host->error;
+            if (c->st_host->done) break;
+        }
+        total_inner += j > dopt->max_inner ? dopt->max_inner : j;
+        // converged inner solve: u <- Phi(u) (solver.jl:501-503)
+        k_copy_if_done<<<eg, 256, 0, c->stream>>>(n2, c->st2, 1, b.v1, b.Phi);
+        c->launches++;
+        stage = next_stage;
+    }
+    if (k > max_outer) {
+        k_set_done<<<1, 32, 0, c->stream>>>(c->st, 3);
+        c->launches++;
+    }
+    // exit: converged -> G(v); stagnated / cap -> best G(v) (solver.jl:611, :617, :631)
+    k_copy_if_done<<<eg, 256, 0, c->stream>>>(n2, c->st, 1, b.v1, b.Gv);
+    k_copy_if_done<<<eg, 256, 0, c->stream>>>(n2, c->st, 2, b.v1, b.vbest);
+    k_copy_if_done<<<eg, 256, 0, c->stream>>>(n2, c->st, 3, b.v1, b.vbest);
+    c->launches += 3;
+    CO_CK(cudaGetLastError());
+    CO_CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(co_solver_state), cudaMemcpyDeviceToHost,
+                          c->stream));
+    CO_CK(cudaStreamSynchronize(c->stream));
+    if (c->st_host->error) return c->st_host->error;
+    if (outer) *outer = k > max_outer ? max_outer : k;
+    if (res) *res = c->st_host->done == 1 ? c->st_host->nrm_r : c->st_host->nrm_best;
+    if (inner) *inner = total_inner;
+    if (r0) *r0 = c->st_host->nrm_r0;
     return CO_OK;
 }

@@ -570,6 +570,7 @@ int co_ensure_capacity(co_ctx *c, int N, int m) {
     int rc;
     if (N > b.cap) {
         int cap = N < 1024 ? 1024 : N;
+        cap = (cap + 255) / 256 * 256;  // packed pair operands are padded to whole tiles
         size_t n2 = 2 * (size_t)cap;
         double **d2[] = {&b.vmid, &b.dv, &b.G, &b.dS, &b.Gv, &b.r, &b.rp, &b.Gp,
                          &b.vbest, &b.v1, &b.v0, &b.vin, &b.dotv, &b.xi};
@@ -595,6 +596,11 @@ int co_ensure_capacity(co_ctx *c, int N, int m) {
         if ((rc = grow(&b.hoff, (size_t)nchunk * c->n_el))) return rc;
         b.nchunk_cap = nchunk;
         b.cap = cap;
+        double **lazy[] = {&b.Gk, &b.Phi, &b.Adef};  // re-created at the new size on use
+        for (double **q : lazy) {
+            if (*q) cudaFree(*q);
+            *q = nullptr;
+        }
         if (b.m_cap > 0) {
             if ((rc = grow(&b.dF, n2 * b.m_cap))) return rc;
             if ((rc = grow(&b.dG, n2 * b.m_cap))) return rc;

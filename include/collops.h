@@ -42,6 +42,8 @@ extern "C" {
 #define CO_FLAG_LOGSQ 1u      /* use_logsq (Parameters.jl:63; functions.jl:9)  */
 #define CO_FLAG_FP32_PAIR 2u  /* gpu_fp32 (Parameters.jl:133): co_collision
                                  runs the mixed FP32 pair sum                  */
+#define CO_FLAG_ONESIDED 4u   /* evaluate every ordered pair (no Newton's-third-
+                                 law symmetric kernels); for comparison runs   */
 
 /* model */
 #define CO_MODEL_LANDAU 0
@@ -144,6 +146,34 @@ int co_step_anderson_dev(co_ctx *ctx, const co_opts *opts, double *v1,
                          double dt, int *iters, double *res, int *n_restarts,
                          double *r0);
 
+/* Options of step_defect! (solver.jl:569-576) beyond co_opts: the inner
+ * tolerance factor eta, the inner-map cap and the outer stagnation window
+ * (SimParameters dc_eta, dc_max_inner, dc_stag_window; Parameters.jl:89-91),
+ * and, for CO_PREC_MIXED, the FP32-stage stall ratio: FP32 outer maps run
+ * while each outer residual is below fp32_stall times the previous one
+ * (<= 0 selects 0.5), then FP64 outer maps take over. */
+typedef struct {
+    double eta;
+    int max_inner;
+    int stag_window;
+    double fp32_stall;
+    int metric64;   /* 1: the frozen metric A comes from the FP64 F+A pair kernel
+                       (COLLMETRIC_FN, the reference's path); 0: F from the
+                       Newton's-third-law kernel and A from an FP32 kernel (A
+                       only shapes the inner model, not the fixed point)      */
+} co_defect_opts;
+
+/* step_defect! (solver.jl:569-634): defect correction around a frozen
+ * metric, Landau only. opts->m, damping, tol, abs_floor, max_iter (outer cap),
+ * stag_rel_tol, use_gonzalez and precision apply. Outputs mirror its return
+ * tuple (outer_iterations, residual, inner_iterations, initial_residual). */
+int co_step_defect(co_ctx *ctx, const co_opts *opts, const co_defect_opts *dopts,
+                   double *v1, const double *v0, const double *w, int N, double S0,
+                   double dt, int *outer, double *res, int *inner, double *r0);
+int co_step_defect_dev(co_ctx *ctx, const co_opts *opts, const co_defect_opts *dopts,
+                       double *v1, const double *v0, const double *w, int N, double S0,
+                       double dt, int *outer, double *res, int *inner, double *r0);
+
 /* Explicit Euler predictor of the time loop (main.jl:233-245):
  * v1 = v + dt * vdot(v) with the model's right-hand side. */
 int co_predictor(co_ctx *ctx, const co_opts *opts, double *v1, const double *v,
@@ -158,6 +188,32 @@ int co_entropy_of_markers_dev(co_ctx *ctx, const double *v, const double *w,
 
 /* Number of kernels this context has launched so far. */
 int co_launch_count(const co_ctx *ctx, unsigned long long *launches);
+
+/* ---- measurement (no counterpart in the reference: its timing is host-side
+ * wall time, main.jl:227, :295; scripts/check_metric_gpu.jl:39-42) ---- */
+
+/* The context's CUDA stream (a cudaStream_t), for callers that time work
+ * with their own events on the launching stream. */
+int co_ctx_stream(const co_ctx *ctx, void **stream);
+
+/* Per-kernel timing of the pair sums with CUDA events recorded around each
+ * launch on the context's stream. */
+typedef struct {
+    double pair64_ms;                    /* summed event time, FP64 pair kernels */
+    unsigned long long pair64_launches;
+    double pair64_pairs;                 /* sum over launches of M (M - 1)      */
+    double pair32_ms;                    /* same for the mixed FP32 kernel       */
+    unsigned long long pair32_launches;
+    double pair32_pairs;
+    unsigned long long maps64, maps32;   /* Picard maps by pair precision       */
+} co_profile_t;
+/* enable != 0 starts (and zeroes) the counters; 0 stops them. */
+int co_profile(co_ctx *ctx, int enable);
+int co_profile_read(co_ctx *ctx, co_profile_t *out);
+
+/* Sustained FMA throughput of this GPU in FLOP/s (2 per FMA), measured by a
+ * register-resident FFMA (fp64 = 0) or DFMA (fp64 = 1) chain kernel. */
+int co_measure_fma_peak(int device, int fp64, double *flops_per_s);
 
 #ifdef __cplusplus
 }

@@ -70,6 +70,8 @@ def _load():
                                   C.c_double, C.c_double]
     lib.om_step_anderson.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp, _dp, C.c_int,
                                      C.c_double, C.c_double, _dp]
+    lib.om_step_defect.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_int, _dp,
+                                   _dp, _dp, C.c_int, C.c_double, C.c_double, _dp]
     lib.om_predictor.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp, _dp, C.c_int, C.c_double]
     _lib = lib
     return lib
@@ -252,6 +254,18 @@ class OracleMesh:
         o = opts.c()
         self.lib.om_step_anderson(self.h, C.byref(o), _d(v1), _d(v0), _d(w), v0.shape[0],
                                   S0, dt, _d(out4))
+        return v1, (int(out4[0]), out4[1], int(out4[2]), out4[3])
+
+    def step_defect(self, opts: Opts, v1, v0, w, S0: float, dt: float, eta: float = 0.05,
+                    max_inner: int = 60, stag_window: int = 5):
+        """step_defect! (solver.jl:569-634) -> (v, (outer, residual, inner, r0))."""
+        v1 = np.array(v1, dtype=np.float64, order="F", copy=True)
+        v0 = _mk(v0)
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        out4 = np.zeros(4)
+        o = opts.c()
+        self.lib.om_step_defect(self.h, C.byref(o), eta, max_inner, stag_window, _d(v1), _d(v0),
+                                _d(w), v0.shape[0], S0, dt, _d(out4))
         return v1, (int(out4[0]), out4[1], int(out4[2]), out4[3])
 
     def predictor(self, opts: Opts, v, w, dt: float) -> np.ndarray:

@@ -834,3 +834,164 @@ void om_predictor(const om_mesh *m, const om_opts *o, double *v1,
     for (int i = 0; i < 2 * N; i++) v1[i] = v[i] + dt * dotv[i];
     free(fc); free(r); free(L); free(G); free(dotv);
 }
+
+/* ---------------------------------------------------------- defect correction */
+
+/* landau_geff! (solver.jl:86-113) at v_in: G_eff and (optionally) v_mid */
+static void landau_geff(const om_mesh *m, int gonzalez, double *Geff, double *vmid,
+                        const double *v_in, const double *v0, const double *w, int N, double S0) {
+    int nd = m->n_dofs;
+    double *dv = malloc(sizeof(double) * 2 * N), *dS = malloc(sizeof(double) * 2 * N);
+    double *Gb = malloc(sizeof(double) * 2 * N);
+    double *fbuf = malloc(sizeof(double) * nd), *r = malloc(sizeof(double) * nd);
+    double *L = malloc(sizeof(double) * nd);
+    for (int i = 0; i < 2 * N; i++) {
+        vmid[i] = 0.5 * (v0[i] + v_in[i]);
+        dv[i] = v_in[i] - v0[i];
+    }
+    entropy_gradient(m, dS, vmid, w, N, fbuf, r, L, Gb);
+    double corr = 0.0;
+    if (gonzalez) {
+        om_l2_project(m, v_in, w, N, fbuf);
+        double S1 = om_entropy(m, fbuf);
+        double dot = 0.0, nrm2 = 0.0;
+        for (int a = 0; a < N; a++) {
+            dot += dv[a] * dS[a] + dv[N + a] * dS[N + a];
+            nrm2 += dv[a] * dv[a] + dv[N + a] * dv[N + a];
+        }
+        corr = nrm2 > 1e-30 ? (S1 - S0 - dot) / nrm2 : 0.0;
+    }
+    for (int a = 0; a < N; a++) {
+        double iw = 1.0 / w[a];
+        Geff[a] = -(dS[a] + corr * dv[a]) * iw;
+        Geff[N + a] = -(dS[N + a] + corr * dv[N + a]) * iw;
+    }
+    free(dv); free(dS); free(Gb); free(fbuf); free(r); free(L);
+}
+
+typedef struct {
+    const om_mesh *m;
+    int gonzalez, N;
+    const double *v0, *w, *Gv, *A, *Gk;
+    double S0, dt;
+    double *Geff, *vmid;
+} frozen_ctx;
+
+/* frozen_map! (solver.jl:585-595) */
+static void frozen_map(frozen_ctx *f, double *out, const double *u) {
+    int N = f->N;
+    landau_geff(f->m, f->gonzalez, f->Geff, f->vmid, u, f->v0, f->w, N, f->S0);
+    for (int a = 0; a < N; a++) {
+        double d1 = f->Geff[a] - f->Gk[a];
+        double d2 = f->Geff[N + a] - f->Gk[N + a];
+        out[a] = f->Gv[a] - f->dt * (f->A[a] * d1 + f->A[N + a] * d2);
+        out[N + a] = f->Gv[N + a] - f->dt * (f->A[N + a] * d1 + f->A[2 * N + a] * d2);
+    }
+}
+
+/* _anderson_inner! (solver.jl:492-526); returns the number of map evaluations */
+static int anderson_inner(frozen_ctx *fc, double *u, double tol, int maxit, int mm,
+                          double damping, double reg_factor) {
+    int n = 2 * fc->N;
+    double *Fu = malloc(sizeof(double) * n), *r = malloc(sizeof(double) * n);
+    double *rp = malloc(sizeof(double) * n), *Fp = malloc(sizeof(double) * n);
+    double *uold = malloc(sizeof(double) * n);
+    double *dF = calloc((size_t)n * mm, sizeof(double)), *dG = calloc((size_t)n * mm, sizeof(double));
+    int hist = 0, slot = 0, ret = maxit;
+    for (int k = 1; k <= maxit; k++) {
+        memcpy(uold, u, sizeof(double) * n);
+        frozen_map(fc, Fu, u);
+        for (int i = 0; i < n; i++) r[i] = Fu[i] - u[i];
+        if (norm2v(r, n) < tol) {
+            memcpy(u, Fu, sizeof(double) * n);
+            ret = k;
+            break;
+        }
+        if (k == 1) {
+            for (int i = 0; i < n; i++) u[i] = damping * Fu[i] + (1 - damping) * uold[i];
+        } else {
+            slot = slot % mm + 1;
+            hist = hist + 1 < mm ? hist + 1 : mm;
+            double *F = dF + (size_t)(slot - 1) * n, *Gc = dG + (size_t)(slot - 1) * n;
+            for (int i = 0; i < n; i++) { F[i] = r[i] - rp[i]; Gc[i] = Fu[i] - Fp[i]; }
+            double ATA[64], ATr[8];
+            for (int a = 0; a < hist; a++) {
+                for (int b = 0; b < hist; b++) {
+                    double s = 0.0;
+                    for (int i = 0; i < n; i++) s += dF[(size_t)a * n + i] * dF[(size_t)b * n + i];
+                    ATA[a * hist + b] = s;
+                }
+                double s = 0.0;
+                for (int i = 0; i < n; i++) s += dF[(size_t)a * n + i] * r[i];
+                ATr[a] = s;
+            }
+            double dm = 0.0;
+            for (int j = 0; j < hist; j++) dm += ATA[j * hist + j];
+            double l2 = reg_factor * dm / hist + 1e-30;
+            for (int j = 0; j < hist; j++) ATA[j * hist + j] += l2;
+            lu_solve(hist, ATA, ATr);
+            for (int i = 0; i < n; i++) {
+                double s = Fu[i];
+                for (int j = 0; j < hist; j++) s += -1.0 * dG[(size_t)j * n + i] * ATr[j];
+                u[i] = damping * s + (1 - damping) * uold[i];
+            }
+        }
+        memcpy(rp, r, sizeof(double) * n);
+        memcpy(Fp, Fu, sizeof(double) * n);
+    }
+    free(Fu); free(r); free(rp); free(Fp); free(uold); free(dF); free(dG);
+    return ret;
+}
+
+/* step_defect! (solver.jl:569-634). out4 = outer, residual, inner, initial residual */
+void om_step_defect(const om_mesh *m, const om_opts *o, double eta, int max_inner,
+                    int stag_window, double *v1, const double *v0, const double *w, int N,
+                    double S0, double dt, double *out4) {
+    int n = 2 * N;
+    double *Geff = malloc(sizeof(double) * n), *vmid = malloc(sizeof(double) * n);
+    double *dotv = malloc(sizeof(double) * n), *A = malloc(sizeof(double) * 3 * N);
+    double *Gv = malloc(sizeof(double) * n), *r = malloc(sizeof(double) * n);
+    double *Gk = malloc(sizeof(double) * n), *vbest = malloc(sizeof(double) * n);
+    double nrm0 = 0.0, nrm_best = INFINITY, nrm_best_window = INFINITY;
+    int inner = 0;
+    memcpy(vbest, v1, sizeof(double) * n);
+    frozen_ctx fc = {m, o->use_gonzalez, N, v0, w, Gv, A, Gk, S0, dt, NULL, NULL};
+    double *fGeff = malloc(sizeof(double) * n), *fvmid = malloc(sizeof(double) * n);
+    fc.Geff = fGeff;
+    fc.vmid = fvmid;
+    for (int k = 1; k <= o->max_iter; k++) {
+        landau_geff(m, o->use_gonzalez, Geff, vmid, v1, v0, w, N, S0);
+        om_collision_metric(m, vmid, w, Geff, N, dotv, A, o->nthreads);
+        for (int i = 0; i < n; i++) {
+            Gv[i] = v0[i] + dt * dotv[i];
+            r[i] = Gv[i] - v1[i];
+        }
+        double nrm = norm2v(r, n);
+        if (k == 1) nrm0 = nrm;
+        if (nrm < nrm_best) {
+            nrm_best = nrm;
+            memcpy(vbest, Gv, sizeof(double) * n);
+        }
+        if (nrm < fmax(o->tol * (norm2v(v1, n) + 1e-30), o->abs_floor)) {
+            memcpy(v1, Gv, sizeof(double) * n);
+            out4[0] = k; out4[1] = nrm; out4[2] = inner; out4[3] = nrm0;
+            goto done;
+        }
+        if (k > stag_window && k % stag_window == 0) {
+            if ((nrm_best_window - nrm_best) / (nrm_best_window + 1e-30) < o->stag_rel_tol) {
+                memcpy(v1, vbest, sizeof(double) * n);
+                out4[0] = k; out4[1] = nrm_best; out4[2] = inner; out4[3] = nrm0;
+                goto done;
+            }
+            nrm_best_window = nrm_best;
+        }
+        memcpy(Gk, Geff, sizeof(double) * n);
+        inner += anderson_inner(&fc, v1, fmax(eta * nrm, 0.5 * o->abs_floor), max_inner, o->m,
+                                o->damping, o->reg_factor);
+    }
+    memcpy(v1, vbest, sizeof(double) * n);
+    out4[0] = o->max_iter; out4[1] = nrm_best; out4[2] = inner; out4[3] = nrm0;
+done:
+    free(Geff); free(vmid); free(dotv); free(A); free(Gv); free(r); free(Gk); free(vbest);
+    free(fGeff); free(fvmid);
+}
