@@ -114,6 +114,9 @@ _SIGNATURES = {
     "co_profile": (C.c_int, [C.c_void_p, C.c_int]),
     "co_profile_read": (C.c_int, [C.c_void_p, C.POINTER(CoProfile)]),
     "co_measure_fma_peak": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
+    "co_collision_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                       C.c_double, C.c_double, C.c_double, C.c_double,
+                                       C.c_void_p]),
 }
 
 

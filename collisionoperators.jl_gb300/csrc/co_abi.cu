@@ -166,6 +166,7 @@ extern "C" const char *co_strerror(int s) {
         case CO_ERR_TIMEOUT: return "device-side wait timed out";
         case CO_ERR_NOMEM: return "device allocation failed";
         case CO_ERR_NODEVICE: return "no CUDA device";
+        case CO_ERR_SIZE: return "N exceeds the 32768-marker limit of co_collision_noalloc";
         default: return "unknown status";
     }
 }

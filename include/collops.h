@@ -37,6 +37,7 @@ extern "C" {
 #define CO_ERR_TIMEOUT 5      /* a bounded device-side wait gave up            */
 #define CO_ERR_NOMEM 6        /* device allocation failed                      */
 #define CO_ERR_NODEVICE 7     /* no CUDA device visible                        */
+#define CO_ERR_SIZE 8         /* N beyond the fixed scratch of co_collision_noalloc */
 
 /* context flags */
 #define CO_FLAG_LOGSQ 1u      /* use_logsq (Parameters.jl:63; functions.jl:9)  */
@@ -185,6 +186,23 @@ int co_predictor_dev(co_ctx *ctx, const co_opts *opts, double *v1,
  * the S0 of the next step (main.jl:228, :298-300). */
 int co_entropy_of_markers_dev(co_ctx *ctx, const double *v, const double *w,
                               int N, double *S);
+
+/* COLLISION_FN for callers that cannot allocate device memory (no
+ * counterpart in the reference). Some hosts own every byte of device memory
+ * themselves -- a Julia process whose CUDA.jl pool manages the GPU, or an
+ * application that must not allocate between time steps -- and cannot create
+ * a co_ctx, which allocates. This entry point allocates nothing: v, w, G and
+ * dot_v are DEVICE pointers in the reference's layout, (lo1, hi1) x (lo2, hi2)
+ * is the domain (bp1[1], bp1[end]) x (bp2[1], bp2[end]), and its scratch is a
+ * fixed 4 MiB __device__ array that every GPU loading the library keeps until
+ * exit. N must be <= 32768 (else CO_ERR_SIZE). The first call on a device sets
+ * up the array's address and should come before any stream capture. All calls
+ * share the array: calls whose kernels overlap on the GPU race and must be
+ * serialised by the caller. Work is enqueued on `stream` (a cudaStream_t, NULL
+ * for the default stream) and not synchronised. FP64, one-sided pair loop. */
+int co_collision_noalloc(const double *v, const double *w, const double *G,
+                         double *dot_v, int N, double lo1, double hi1, double lo2,
+                         double hi2, void *stream);
 
 /* Number of kernels this context has launched so far. */
 int co_launch_count(const co_ctx *ctx, unsigned long long *launches);
