@@ -9,8 +9,10 @@ N_QUAD 6. Markers are seeded synthetic data (numpy default_rng(42)).
 
 One "step" = one time step of the reference's loop (main.jl:226-300): the
 explicit predictor, step_anderson! to convergence, and the entropy S0 of the
-new state for the next step. `value` times the headline form (mixed: FP32 pair
-maps, FP64 exit Picard map) with inputs resident in HBM; `plain_fp64` times the
+new state for the next step. `value` times the headline form -- mixed
+precision (FP32 pair maps, then double-single pair maps for the FP64 stage)
+with the learned warm start (falling back to the predictor when its first
+residual is larger) and defect correction -- with inputs resident in HBM; `plain_fp64` times the
 plain FP64 form from the same state; `e2e` drives the headline form through the
 host-pointer C ABI with host<->device copies inside the timed region.
 Each timed step is bracketed by CUDA events on the library's stream; a 256 MB
@@ -190,7 +192,7 @@ def fp64_maps_from_profile():
     return None
 
 
-def cpu_baseline(cfg, maps_per_step, maps_src, rows_sample=1024):
+def cpu_baseline(cfg, maps_per_step, maps_src, rows_sample=32768):
     threads = os.cpu_count() or 1
     v, w = markers(cfg, cfg["seed"])
     per_map, d = oracle_map_sample(cfg, v, w, rows_sample, threads)
@@ -238,8 +240,7 @@ def run_gpu(args, cfg):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
     def opts(prec):
-        return p.opts(precision=co.CO_PREC_MIXED if prec == "mixed" else co.CO_PREC_FP64,
-                      mixed_floor=args.mixed_floor)
+        return p.opts(precision=co._PREC[prec], mixed_floor=args.mixed_floor)
 
     def entropy(x):
         S = C.c_double()
@@ -249,12 +250,25 @@ def run_gpu(args, cfg):
 
     dopt = co.CoDefectOpts(args.dc_eta, args.dc_max_inner, args.dc_stag_window, 0.5, 0)
 
-    def one_step(x, S0, prec, solver=None):
-        """predictor + the implicit solve (+ S of the new state); returns new x, S, info."""
+    warm = None
+    if args.warmstart == "learned":
+        from collops import learned
+        if os.path.exists(args.warmstart_file):
+            warm = learned.WarmStart.load(args.warmstart_file, device=local)
+    ws_stats = {"used": 0, "steps": 0}
+
+    def one_step(x, S0, prec, solver=None, learned_start=True):
+        """warm start (learned proposal or the explicit predictor) + the implicit
+        solve (+ S of the new state); returns new x, S, info."""
         solver = solver or args.solver
         o = opts(prec)
-        co._check(lib.co_predictor_dev(h, C.byref(o), v1.data_ptr(), x.data_ptr(), w.data_ptr(),
-                                       N, dt), "co_predictor_dev")
+        if warm is not None and learned_start and solver == args.solver:
+            used, _rl, _rp = warm.propose(ws, o, x, w, S0, dt, v1)
+            ws_stats["used"] += int(used)
+            ws_stats["steps"] += 1
+        else:
+            co._check(lib.co_predictor_dev(h, C.byref(o), v1.data_ptr(), x.data_ptr(),
+                                           w.data_ptr(), N, dt), "co_predictor_dev")
         it, nrs = C.c_int(), C.c_int()
         res, r0 = C.c_double(), C.c_double()
         if solver == "defect":
@@ -335,7 +349,7 @@ def run_gpu(args, cfg):
         lib.co_profile_read(h, C.byref(prof64))
         lib.co_profile(h, 0)
         # one headline step from the same start for the velocity comparison
-        xm, Sm, _info = one_step(x_start.clone(), S_start, args.form)
+        xm, Sm, info_m = one_step(x_start.clone(), S_start, args.form)
         x0 = x_start.cpu().numpy()
         a64, am = xp.cpu().numpy(), xm.cpu().numpy()
         wn = w.cpu().numpy()
@@ -345,7 +359,8 @@ def run_gpu(args, cfg):
                 E0 = 0.5 * (wn * (x0 ** 2).sum(0)).sum()
                 dE = abs(0.5 * (wn * (a ** 2).sum(0)).sum() - E0) / E0
                 return float(dP), float(dE)
-            acc = dict(vel_diff_vs_plain_fp64=float(np.abs(am - a64).max() / np.abs(a64).max()),
+            acc = dict(headline_step=dict(iterations=info_m[0], residual=info_m[1]),
+                       vel_diff_vs_plain_fp64=float(np.abs(am - a64).max() / np.abs(a64).max()),
                        fp64_map_residual_headline=fp64_residual(xm, x_start, S_start),
                        fp64_map_residual_plain=fp64_residual(xp, x_start, S_start),
                        momentum_drift_mixed=drift(am)[0], energy_drift_rel_mixed=drift(am)[1],
@@ -414,7 +429,19 @@ def run_gpu(args, cfg):
 
     r32 = roof(prof.pair32_ms, prof.pair32_launches, prof.pair32_pairs, peak32.value, "fp32")
     r64 = roof(prof.pair64_ms, prof.pair64_launches, prof.pair64_pairs, peak64.value, "fp64")
-    dominant = r32 if (prof.pair32_ms >= prof.pair64_ms and r32) else r64
+    rds = roof(prof.pairds_ms, prof.pairds_launches, prof.pairds_pairs, peak32.value, "fp32")
+    if rds:
+        rds["kernel"] = "k_pair_ds_sym"
+        rds["fp64_equivalent_frac"] = round(rds["achieved"] / (peak64.value / 1e12), 3)
+        rds["note"] = ("double-single (FP32 head+tail) arithmetic: 23 FP64-equivalent flops per "
+                       "pair, executed as ~130 FP32 instructions; frac is against the FP32 peak, "
+                       "fp64_equivalent_frac against the measured FP64 peak")
+    if r32:
+        r32["kernel"] = "k_pair32_sym"
+    if r64:
+        r64["kernel"] = "k_pair64_sym"
+    cands = [(prof.pair32_ms, r32), (prof.pair64_ms, r64), (prof.pairds_ms, rds)]
+    dominant = max((c for c in cands if c[1]), key=lambda c: c[0], default=(0, None))[1]
     traffic = load_traffic()
     if dominant and traffic.get(dominant["kernel"]) is not None:
         dominant["traffic"] = traffic[dominant["kernel"]]
@@ -436,7 +463,9 @@ def run_gpu(args, cfg):
         "metric": METRIC, "value": round(job_ms, 2), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(job_ms, 2),
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-        "dtype": "fp32 pair arithmetic + fp64" if args.form == "mixed" else "fp64",
+        "dtype": {"mixed": "fp32 pair maps + fp64 pair maps",
+                  "mixed_ds": "fp32 pair maps + double-single (fp32x2) pair maps",
+                  "fp64": "fp64"}[args.form] + "; fp64 projection, mass solve, Gonzalez, solver",
         "data": "synthetic: seeded anisotropic Gaussian markers (numpy default_rng)",
         "config": {"workload": cfg["name"], "form": args.form, "solver": args.solver, "N": N,
                    "mesh": f"{cfg['n_el']}x{cfg['n_el']} P2 on [{cfg['lo']},{cfg['hi']}]^2",
@@ -447,9 +476,12 @@ def run_gpu(args, cfg):
         "step_ms": [round(t, 1) for t in times],
         "iterations": [i[0] for i in infos], "residuals": [i[1] for i in infos],
         "inner_or_restarts": [i[2] for i in infos],
-        "maps": {"fp32": prof.maps32, "fp64": prof.maps64},
+        "maps": {"fp32": prof.maps32, "fp64": prof.maps64, "double_single": prof.mapsds},
         "plain_fp64": plain, "accuracy": acc,
-        "roofline": dominant, "roofline_fp64": r64,
+        "warmstart": ({"kind": "learned MLP (BF16, own kernels)", "file": os.path.relpath(
+            args.warmstart_file, ROOT), "learned_start_used": ws_stats["used"],
+            "steps": ws_stats["steps"]} if warm is not None else {"kind": "explicit predictor"}),
+        "roofline": dominant, "roofline_fp64": r64, "roofline_fp32": r32, "roofline_ds": rds,
         "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": int(n_launch),
     }
     if plain:
@@ -517,15 +549,18 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--form", choices=["mixed", "fp64"], default="mixed")
+    ap.add_argument("--form", choices=["mixed_ds", "mixed", "fp64"], default="mixed_ds")
     ap.add_argument("--solver", choices=["defect", "anderson"], default="defect")
+    ap.add_argument("--warmstart", choices=["learned", "euler"], default="learned")
+    ap.add_argument("--warmstart-file", default=os.path.join(
+        PKG, "collops", "warmstart_c3.npz"))
     ap.add_argument("--dc-eta", type=float, default=0.05)
     ap.add_argument("--dc-max-inner", type=int, default=60)
     ap.add_argument("--dc-stag-window", type=int, default=5)
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--mixed-floor", type=float, default=0.0)
-    ap.add_argument("--cpu-rows", type=int, default=1024)
+    ap.add_argument("--cpu-rows", type=int, default=32768)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--N", type=int, default=None, help="override the marker count (tests)")
     args = ap.parse_args(argv)

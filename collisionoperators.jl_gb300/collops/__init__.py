@@ -36,7 +36,8 @@ _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 
 CO_MODEL_LANDAU, CO_MODEL_LB = 0, 1
-CO_PREC_FP64, CO_PREC_MIXED = 0, 1
+CO_PREC_FP64, CO_PREC_MIXED, CO_PREC_MIXED_DS = 0, 1, 2
+_PREC = {"fp64": CO_PREC_FP64, "mixed": CO_PREC_MIXED, "mixed_ds": CO_PREC_MIXED_DS}
 CO_FLAG_LOGSQ, CO_FLAG_FP32_PAIR, CO_FLAG_ONESIDED = 1, 2, 4
 
 
@@ -67,13 +68,21 @@ class CoProfile(C.Structure):
     _fields_ = [("pair64_ms", C.c_double), ("pair64_launches", C.c_ulonglong),
                 ("pair64_pairs", C.c_double), ("pair32_ms", C.c_double),
                 ("pair32_launches", C.c_ulonglong), ("pair32_pairs", C.c_double),
-                ("maps64", C.c_ulonglong), ("maps32", C.c_ulonglong)]
+                ("maps64", C.c_ulonglong), ("maps32", C.c_ulonglong),
+                ("pairds_ms", C.c_double), ("pairds_launches", C.c_ulonglong),
+                ("pairds_pairs", C.c_double), ("mapsds", C.c_ulonglong)]
 
 
 class CoDefectOpts(C.Structure):
     """co_defect_opts of include/collops.h."""
     _fields_ = [("eta", C.c_double), ("max_inner", C.c_int), ("stag_window", C.c_int),
                 ("fp32_stall", C.c_double), ("metric64", C.c_int)]
+
+
+class CoBatchInstance(C.Structure):
+    """co_batch_instance of include/collops.h."""
+    _fields_ = [("bp1", C.POINTER(C.c_double)), ("nb1", C.c_int), ("bp2", C.POINTER(C.c_double)),
+                ("nb2", C.c_int), ("model", C.c_int), ("nu", C.c_double), ("N", C.c_int)]
 
 
 # (name, restype, argtypes) of every entry point in include/collops.h
@@ -114,6 +123,33 @@ _SIGNATURES = {
     "co_profile": (C.c_int, [C.c_void_p, C.c_int]),
     "co_profile_read": (C.c_int, [C.c_void_p, C.POINTER(CoProfile)]),
     "co_measure_fma_peak": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
+    "co_batch_create": (C.c_int, [C.POINTER(CoBatchInstance), C.c_int, C.c_int, C.c_uint,
+                                  C.c_int, C.POINTER(C.c_void_p)]),
+    "co_batch_destroy": (C.c_int, [C.c_void_p]),
+    "co_batch_tune": (C.c_int, [C.c_void_p, _ip, _ip, _ip, _dp]),
+    "co_batch_step_dev": (C.c_int, [C.c_void_p, C.POINTER(CoOpts), C.c_void_p, C.c_void_p,
+                                    C.c_void_p, _dp, C.c_double, C.c_int, _ip, _dp]),
+    "co_batch_predictor_dev": (C.c_int, [C.c_void_p, C.POINTER(CoOpts), C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_double]),
+    "co_batch_entropy_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, _dp]),
+    "co_batch_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_ulonglong)]),
+    "co_mlp_create": (C.c_int, [C.c_int, C.c_int, C.c_uint, C.c_int, C.POINTER(C.c_void_p)]),
+    "co_mlp_destroy": (C.c_int, [C.c_void_p]),
+    "co_mlp_num_params": (C.c_int, [C.c_void_p, _ip]),
+    "co_mlp_set_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    "co_mlp_get_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    "co_mlp_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "co_mlp_gradients": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                   C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "co_mlp_train_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_float,
+                                    C.POINTER(C.c_float)]),
+    "co_warmstart_features_dev": (C.c_int, [C.c_void_p, C.POINTER(CoOpts), C.c_void_p,
+                                            C.c_void_p, C.c_int, C.c_double, C.c_void_p,
+                                            C.c_void_p]),
+    "co_warmstart_apply_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                         C.c_double, _dp, _dp, C.c_void_p]),
+    "co_picard_residual_dev": (C.c_int, [C.c_void_p, C.POINTER(CoOpts), C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_int, C.c_double, C.c_double, _dp]),
     "co_collision_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                        C.c_double, C.c_double, C.c_double, C.c_double,
                                        C.c_void_p]),
@@ -203,7 +239,7 @@ class SimParameters:
                  stag_rel_tol=self.stag_rel_tol, damp_decay_start=self.damp_decay_start,
                  damp_decay_factor=self.damp_decay_factor, restart_factor=-1.0,
                  damping=self.damping, reg_factor=1e-10,
-                 precision=CO_PREC_MIXED if self.precision == "mixed" else CO_PREC_FP64,
+                 precision=_PREC[self.precision],
                  mixed_floor=self.mixed_floor)
         d.update(kw)
         return CoOpts(**d)
@@ -412,7 +448,7 @@ def picard_map(ws: Workspace, v_out, v_in, v0, w_parts, S0: float, dt: float, *,
     N = v0.shape[0]
     kw = {}
     if precision is not None:
-        kw["precision"] = CO_PREC_MIXED if precision == "mixed" else CO_PREC_FP64
+        kw["precision"] = _PREC[precision]
     o = _opts(ws, use_gonzalez, **kw)
     _check(ws.lib.co_picard_map(ws.h, C.byref(o), _p(_out(v_out, (N, 2), "v_out")),
                                 _p(_markers(v_in, N, "v_in")), _p(v0),
@@ -438,8 +474,7 @@ def step_anderson(ws: Workspace, v1, v0, w_parts, S0: float, dt: float, *, m: in
                   restart_factor=restart_factor if np.isfinite(restart_factor) else -1.0,
                   damping=damping, reg_factor=reg_factor, use_anderson=int(use_anderson),
                   use_gonzalez=int(use_gonzalez), exit_picard_step=int(exit_picard_step),
-                  precision=CO_PREC_MIXED if precision == "mixed" else CO_PREC_FP64,
-                  mixed_floor=mixed_floor)
+                  precision=_PREC[precision], mixed_floor=mixed_floor)
     it, nrs = C.c_int(), C.c_int()
     res, r0 = C.c_double(), C.c_double()
     _check(ws.lib.co_step_anderson(ws.h, C.byref(o), _p(v1), _p(v0),
@@ -460,7 +495,7 @@ def step_defect(ws: Workspace, v1, v0, w_parts, S0: float, dt: float, *, m: int 
     v1 = _out(v1, (N, 2), "v1")
     o = ws.p.opts(m=m, max_iter=max_iter, tol=tol, abs_floor=abs_floor, damping=damping,
                   stag_rel_tol=stag_rel_tol, use_gonzalez=int(use_gonzalez),
-                  precision=CO_PREC_MIXED if precision == "mixed" else CO_PREC_FP64)
+                  precision=_PREC[precision])
     d = CoDefectOpts(eta, max_inner, stag_window, fp32_stall, int(metric64))
     it, inner = C.c_int(), C.c_int()
     res, r0 = C.c_double(), C.c_double()
@@ -474,7 +509,7 @@ def predictor(ws: Workspace, v1, v_parts, w_parts, dt: float, precision: str = "
     """Explicit predictor of the time loop (main.jl:233-245): v1 = v + dt vdot(v)."""
     v = _markers(v_parts, name="v_parts")
     N = v.shape[0]
-    o = ws.p.opts(precision=CO_PREC_MIXED if precision == "mixed" else CO_PREC_FP64)
+    o = ws.p.opts(precision=_PREC[precision])
     _check(ws.lib.co_predictor(ws.h, C.byref(o), _p(_out(v1, (N, 2), "v1")), _p(v),
                                _p(_vec(w_parts, N, "w_parts")), N, dt), "co_predictor")
 
@@ -505,3 +540,73 @@ def enable_gpu(p: SimParameters) -> Hooks:
             h.COLLISION_FN = compute_collision_gpu
             h.COLLMETRIC_FN = compute_collision_metric_gpu
     return h
+
+
+class Batch:
+    """Many independent ensembles advanced together (co_batch_*): one engine,
+    one stream, one batched pair-sum launch per Picard iteration for all Landau
+    instances, CUDA-graph replay of the iteration. `instances` is a list of
+    dicts with keys bp1, bp2, model ("landau" | "lb"), nu, N. Marker arrays are
+    torch CUDA tensors of the concatenated per-instance (2, N_i) blocks."""
+
+    def __init__(self, instances, n_quad: int = 6, device: int = 0):
+        self.lib = load_library()
+        self._keep = []
+        arr = (CoBatchInstance * len(instances))()
+        for k, d in enumerate(instances):
+            b1 = np.ascontiguousarray(d["bp1"], dtype=np.float64)
+            b2 = np.ascontiguousarray(d["bp2"], dtype=np.float64)
+            self._keep += [b1, b2]
+            arr[k] = CoBatchInstance(_p(b1), len(b1), _p(b2), len(b2),
+                                     CO_MODEL_LB if d.get("model") == "lb" else CO_MODEL_LANDAU,
+                                     float(d.get("nu", 1.0)), int(d["N"]))
+        h = C.c_void_p()
+        self.h = None
+        _check(self.lib.co_batch_create(arr, len(instances), n_quad, 0, device, C.byref(h)),
+               "co_batch_create")
+        self.h = h
+        self.n = len(instances)
+        self.N = [int(d["N"]) for d in instances]
+        self.offsets = np.concatenate([[0], np.cumsum(self.N)]).astype(np.int64)
+
+    def close(self):
+        if self.h is not None:
+            self.lib.co_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def tune(self):
+        W, KC, grid = C.c_int(), C.c_int(), C.c_int()
+        ms = C.c_double()
+        _check(self.lib.co_batch_tune(self.h, C.byref(W), C.byref(KC), C.byref(grid),
+                                      C.byref(ms)), "co_batch_tune")
+        return dict(warps=W.value, chunk=KC.value, grid=grid.value, pair_ms=ms.value)
+
+    def entropy(self, v, w):
+        S = np.zeros(self.n)
+        _check(self.lib.co_batch_entropy_dev(self.h, v.data_ptr(), w.data_ptr(), _p(S)),
+               "co_batch_entropy_dev")
+        return S
+
+    def predictor(self, opts: CoOpts, v1, v, w, dt: float):
+        _check(self.lib.co_batch_predictor_dev(self.h, C.byref(opts), v1.data_ptr(), v.data_ptr(),
+                                               w.data_ptr(), dt), "co_batch_predictor_dev")
+
+    def step(self, opts: CoOpts, v1, v0, w, S0, dt: float, use_graph: bool = True):
+        S0 = np.ascontiguousarray(S0, dtype=np.float64)
+        it = (C.c_int * self.n)()
+        res = np.zeros(self.n)
+        _check(self.lib.co_batch_step_dev(self.h, C.byref(opts), v1.data_ptr(), v0.data_ptr(),
+                                          w.data_ptr(), _p(S0), dt, int(use_graph), it, _p(res)),
+               "co_batch_step_dev")
+        return list(it), res
+
+    def launch_count(self) -> int:
+        n = C.c_ulonglong()
+        _check(self.lib.co_batch_launch_count(self.h, C.byref(n)), "co_batch_launch_count")
+        return n.value

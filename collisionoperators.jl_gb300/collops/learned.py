@@ -1,0 +1,201 @@
+"""Learned warm start of the implicit step.
+
+A small MLP (9 -> 64 -> 64 -> 64 -> 2, GELU, BF16 weights, FP32 accumulation;
+the kernels are this library's own, see co_mlp.cu) maps per-marker features at
+the start of a step to the normalised correction of the explicit predictor,
+    delta = (v_converged - v_Euler) / dt^2,
+the form of warm start the reference planned ("Euler + dt^2 * delta" MLP
+correction, Parameters.jl:108-112; its warmstart_nn.jl is not in the tree).
+
+The fixed-point map stays the judge: `propose` returns the learned iterate only
+when its first Picard residual (one map at the solver's precision) is smaller
+than that of the plain predictor; otherwise the predictor is used.
+
+Training data comes from the solver itself: `generate_pairs` runs time steps
+and records (features at the step start, delta of the converged step).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import CollopsError, CoOpts, Workspace, _check, _p, load_library
+
+N_IN, N_OUT = 9, 2
+
+
+class MLP:
+    """The network on one device (co_mlp_*)."""
+
+    def __init__(self, seed: int = 0, device: int = 0, n_in: int = N_IN, n_out: int = N_OUT):
+        self.lib = load_library()
+        h = C.c_void_p()
+        self.h = None
+        _check(self.lib.co_mlp_create(n_in, n_out, seed, device, C.byref(h)), "co_mlp_create")
+        self.h = h
+        P = C.c_int()
+        _check(self.lib.co_mlp_num_params(self.h, C.byref(P)), "co_mlp_num_params")
+        self.P = P.value
+        self.n_in, self.n_out = n_in, n_out
+
+    def close(self):
+        if self.h is not None:
+            self.lib.co_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def get_params(self) -> np.ndarray:
+        out = np.zeros(self.P, dtype=np.float32)
+        _check(self.lib.co_mlp_get_params(self.h, out.ctypes.data_as(C.POINTER(C.c_float))),
+               "co_mlp_get_params")
+        return out
+
+    def set_params(self, p) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.P
+        _check(self.lib.co_mlp_set_params(self.h, p.ctypes.data_as(C.POINTER(C.c_float))),
+               "co_mlp_set_params")
+
+    def forward(self, X, Y) -> None:
+        """X (B, n_in) and Y (B, n_out): float32 CUDA tensors."""
+        _check(self.lib.co_mlp_forward(self.h, X.data_ptr(), X.shape[0], Y.data_ptr(), None),
+               "co_mlp_forward")
+
+    def gradients(self, X, T):
+        g = np.zeros(self.P, dtype=np.float32)
+        loss = C.c_float()
+        _check(self.lib.co_mlp_gradients(self.h, X.data_ptr(), T.data_ptr(), X.shape[0],
+                                         g.ctypes.data_as(C.POINTER(C.c_float)), C.byref(loss)),
+               "co_mlp_gradients")
+        return g, loss.value
+
+    def train_step(self, X, T, lr: float) -> float:
+        loss = C.c_float()
+        _check(self.lib.co_mlp_train_step(self.h, X.data_ptr(), T.data_ptr(), X.shape[0], lr,
+                                          C.byref(loss)), "co_mlp_train_step")
+        return loss.value
+
+
+def features(ws: Workspace, opts: CoOpts, v, w, dt: float):
+    """(X float32 (N, 9), v_pred) on the device for markers v (torch (2, N))."""
+    import torch
+    N = v.shape[1]
+    X = torch.empty((N, N_IN), dtype=torch.float32, device=v.device)
+    vp = torch.empty_like(v)
+    _check(ws.lib.co_warmstart_features_dev(ws.h, C.byref(opts), v.data_ptr(), w.data_ptr(), N,
+                                            dt, vp.data_ptr(), X.data_ptr()),
+           "co_warmstart_features_dev")
+    return X, vp
+
+
+class WarmStart:
+    """Normalisation + network; `propose` implements the learned warm start."""
+
+    def __init__(self, mlp: MLP | None = None, device: int = 0):
+        self.mlp = mlp or MLP(device=device)
+        self.xm = np.zeros(N_IN)
+        self.xs = np.ones(N_IN)
+        self.tm = np.zeros(N_OUT)
+        self.ts = np.ones(N_OUT)
+
+    def fit(self, X: np.ndarray, T: np.ndarray, epochs: int = 20, batch: int = 8192,
+            lr: float = 2e-3, seed: int = 0, device: int = 0):
+        """Train on the GPU with the library's kernels; returns the loss history."""
+        import torch
+        self.xm, self.xs = X.mean(0), X.std(0) + 1e-12
+        self.tm, self.ts = T.mean(0), T.std(0) + 1e-30
+        Xn = torch.from_numpy(((X - self.xm) / self.xs).astype(np.float32)).cuda(device)
+        Tn = torch.from_numpy(((T - self.tm) / self.ts).astype(np.float32)).cuda(device)
+        rng = np.random.default_rng(seed)
+        hist = []
+        n = X.shape[0]
+        for ep in range(epochs):
+            perm = torch.from_numpy(rng.permutation(n)).cuda(device)
+            tot, cnt = 0.0, 0
+            for s in range(0, n - batch + 1, batch):
+                idx = perm[s:s + batch]
+                tot += self.mlp.train_step(Xn[idx].contiguous(), Tn[idx].contiguous(),
+                                           lr * (0.5 ** (ep // max(1, epochs // 3))))
+                cnt += 1
+            hist.append(tot / max(cnt, 1))
+        return hist
+
+    def predict_delta(self, X):
+        """Normalised features -> delta (float32 CUDA tensors)."""
+        import torch
+        Xn = ((X - torch.from_numpy(self.xm.astype(np.float32)).to(X.device)) /
+              torch.from_numpy(self.xs.astype(np.float32)).to(X.device)).contiguous()
+        Y = torch.empty((X.shape[0], N_OUT), dtype=torch.float32, device=X.device)
+        self.mlp.forward(Xn, Y)
+        return Y
+
+    def propose(self, ws: Workspace, opts: CoOpts, v, w, S0: float, dt: float, v1_out):
+        """Fill v1_out with the initial iterate: the learned proposal if its first
+        residual is smaller than the predictor's, else the predictor. Returns
+        (used_learned, residual_learned, residual_predictor)."""
+        import torch
+        X, vp = features(ws, opts, v, w, dt)
+        Y = self.predict_delta(X)
+        N = v.shape[1]
+        vl = torch.empty_like(v)
+        sc = np.ascontiguousarray(self.ts, dtype=np.float64)
+        sh = np.ascontiguousarray(self.tm, dtype=np.float64)
+        _check(ws.lib.co_warmstart_apply_dev(ws.h, vp.data_ptr(), Y.data_ptr(), N, dt, _p(sc),
+                                             _p(sh), vl.data_ptr()), "co_warmstart_apply_dev")
+        rl, rp = C.c_double(), C.c_double()
+        _check(ws.lib.co_picard_residual_dev(ws.h, C.byref(opts), vl.data_ptr(), v.data_ptr(),
+                                             w.data_ptr(), N, S0, dt, C.byref(rl)),
+               "co_picard_residual_dev")
+        _check(ws.lib.co_picard_residual_dev(ws.h, C.byref(opts), vp.data_ptr(), v.data_ptr(),
+                                             w.data_ptr(), N, S0, dt, C.byref(rp)),
+               "co_picard_residual_dev")
+        use = rl.value < rp.value
+        v1_out.copy_(vl if use else vp)
+        return use, rl.value, rp.value
+
+    def save(self, path: str) -> None:
+        np.savez_compressed(path, params=self.mlp.get_params(), xm=self.xm, xs=self.xs,
+                            tm=self.tm, ts=self.ts)
+
+    @classmethod
+    def load(cls, path: str, device: int = 0) -> "WarmStart":
+        z = np.load(path)
+        ws = cls(device=device)
+        ws.mlp.set_params(z["params"])
+        ws.xm, ws.xs, ws.tm, ws.ts = z["xm"], z["xs"], z["tm"], z["ts"]
+        return ws
+
+
+def generate_pairs(ws: Workspace, opts: CoOpts, v, w, dt: float, steps: int, solve):
+    """Run `steps` time steps from v (torch (2, N)); `solve(v1, v, S0)` performs
+    the implicit step in place on v1. Returns (X, T) numpy arrays: features at
+    each step start and delta = (v_converged - v_pred)/dt^2, plus the final v."""
+    import torch
+    Xs, Ts = [], []
+    x = v.clone()
+    for _ in range(steps):
+        S0 = entropy_of(ws, x, w)
+        X, vp = features(ws, opts, x, w, dt)
+        v1 = vp.clone()
+        solve(v1, x, S0)
+        delta = ((v1 - vp) / (dt * dt)).T.contiguous()
+        Xs.append(X.cpu().numpy())
+        Ts.append(delta.cpu().numpy())
+        x = v1
+    return np.concatenate(Xs), np.concatenate(Ts), x
+
+
+def entropy_of(ws: Workspace, v, w) -> float:
+    S = C.c_double()
+    _check(ws.lib.co_entropy_of_markers_dev(ws.h, v.data_ptr(), w.data_ptr(), v.shape[1],
+                                            C.byref(S)), "co_entropy_of_markers_dev")
+    return S.value
+
+
+__all__ = ["MLP", "WarmStart", "features", "generate_pairs", "entropy_of", "CollopsError"]

@@ -20,8 +20,6 @@
 int co_spline_configure(co_ctx *c);
 int co_step_anderson_buffers(co_ctx *c, const co_opts *o, int N, double S0, double dt,
                              int *iters, double *res, int *nrs, double *r0);
-int co_predictor_buffers(co_ctx *c, const co_opts *o, int precision, const double *v, int N,
-                         double dt, double *out);
 
 #define CO_RED_CAP 1024
 #define CO_RED_COMPS 16
@@ -178,7 +176,7 @@ static void free_ctx(co_ctx *c) {
                     c->mb.vmid, c->mb.dv, c->mb.G, c->mb.dS, c->mb.Gv, c->mb.r, c->mb.rp,
                     c->mb.Gp, c->mb.vbest, c->mb.v1, c->mb.v0, c->mb.w, c->mb.vin, c->mb.dotv,
                     c->mb.cell, c->mb.inv, c->mb.xi, c->mb.perm, c->mb.scell, c->mb.sw,
-                    c->mb.sphi, c->mb.px, c->mb.pg, c->mb.pw, c->mb.pf_x, c->mb.pf_g, c->mb.pf_w,
+                    c->mb.sphi, c->mb.px, c->mb.pg, c->mb.pw, c->mb.pf_x, c->mb.pf_g, c->mb.pf_w, c->mb.pf_wl,
                     c->mb.pdot, c->mb.pA, c->mb.part, c->mb.hist, c->mb.hoff, c->mb.count,
                     c->mb.cstart, c->mb.red, c->mb.dF, c->mb.dG, c->mb.Gk, c->mb.Phi,
                     c->mb.Adef, c->st2};
@@ -288,6 +286,10 @@ extern "C" int co_ctx_create(const double *bp1, int nb1, const double *bp2, int 
     return CO_OK;
 }
 
+void co_ctx_destroy_detached(co_ctx *c) {
+    if (c) free_ctx(c);
+}
+
 extern "C" int co_ctx_destroy(co_ctx *c) {
     if (!c) return CO_ERR_ARG;
     cudaSetDevice(c->device);
@@ -348,8 +350,8 @@ static int check_opts(const co_opts *o) {
     if (!o) return CO_ERR_ARG;
     if (o->model != CO_MODEL_LANDAU && o->model != CO_MODEL_LB) return CO_ERR_ARG;
     if (o->m < 1 || o->m > CO_MAX_M || o->max_iter < 1 || o->stag_window < 1) return CO_ERR_ARG;
-    if (o->precision != CO_PREC_FP64 && o->precision != CO_PREC_MIXED) return CO_ERR_ARG;
-    if (o->model == CO_MODEL_LB && o->precision == CO_PREC_MIXED) return CO_ERR_ARG;
+    if (o->precision < CO_PREC_FP64 || o->precision > CO_PREC_MIXED_DS) return CO_ERR_ARG;
+    if (o->model == CO_MODEL_LB && o->precision != CO_PREC_FP64) return CO_ERR_ARG;
     return CO_OK;
 }
 

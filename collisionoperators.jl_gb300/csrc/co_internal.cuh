@@ -30,6 +30,7 @@ struct co_solver_state {
     int history, slot;   // Anderson window (solver.jl:320-321)
     int n_restart;
     int k64;             // defect correction: FP64 outer maps so far
+    int finished;        // batch engine: the exit copy of this instance is done
     int done;            // 0 running, 1 converged, 2 stagnated, 3 max_iter
     int path;            // 0 damped Picard, 1 Anderson, for the current k
     int improved;        // nrm_r < nrm_best at the current k
@@ -58,7 +59,7 @@ struct co_bufs {
     double *pw;
     float4 *pf_x;        // {x1h, x2h, x1l, x2l}
     float4 *pf_g;        // {g1h, g2h, g1l, g2l}
-    float *pf_w;
+    float *pf_w, *pf_wl; // weight head / tail
     double *pdot;        // packed vdot (2 x cap)
     double *pA;          // packed metric A (3 x cap)
     double *part;        // slice partials of the pair kernels
@@ -105,7 +106,10 @@ struct co_ctx {
     unsigned long long launches;
     // pair-kernel profiling (co_prof.cu)
     struct co_prof *prof;
-    unsigned long long maps64, maps32;
+    unsigned long long maps64, maps32, mapsds;
+    // batch membership (co_batch): marker count and whether the instance has a pair sum
+    int batch_N, batch_landau;
+    int lb_two_pass;          // LB drift in two launches (capturable) instead of cooperative
 };
 
 // ------------------------------------------------------------- helpers
@@ -131,20 +135,45 @@ int co_grad_L_dev(co_ctx *c, const double *x, int N, const double *L, double *G,
 int co_loggrad_dev(co_ctx *c, const double *x, int N, const double *f, double *g,
                    const double *w, const double *dv, double *red);
 int co_mid_dv(co_ctx *c, const double *vin, const double *v0, int N);
+int co_features_dev(co_ctx *c, const double *x, int N, float *X);
 
 // ------------------------------------------------------------- pair stage
 // (co_pair.cu)
 int co_pair_fp64(co_ctx *c, int M, int with_metric);   // packed -> pdot (and pA)
 int co_pair_fp32(co_ctx *c, int M);                    // packed FP32 -> pdot
+int co_pair_ds(co_ctx *c, int M);                      // packed FP32 head/tail -> pdot,
+                                                       // double-single arithmetic
 int co_pack_landau(co_ctx *c, int N, int Mub, int precision, int gonzalez);
 int co_pack_plain(co_ctx *c, int N, int Mub, int precision, const double *x, const double *G);
 int co_unpack_A(co_ctx *c, int N, double *A);
 int co_metric32(co_ctx *c, int Mub);   // FP32 metric A (3 x ld in pA) from pf_x/pf_w
+int co_predictor_buffers(co_ctx *c, const co_opts *o, int precision, const double *v, int N,
+                         double dt, double *out);
+void co_ctx_destroy_detached(co_ctx *c);   // free a context whose stream/state it does not own
 int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *dopt, int N,
                            double S0, double dt, int *outer, double *res, int *inner, double *r0);
-#define CO_PREC_BOTH 2                  // pack both FP64 and FP32 operands
+#define CO_PREC_BOTH 3                  // pack both FP64 and FP32 operands (internal)
+// packed-operand sets a precision needs: 1 = FP64 arrays, 2 = FP32 head/tail arrays
+static inline int co_pack_mode(int precision) {
+    return precision == CO_PREC_FP64 ? 1 : precision == CO_PREC_BOTH ? 3 : 2;
+}
 int co_unpack_update(co_ctx *c, int N, double dt, double *Gv, const double *v0,
                      const double *v1, double *r, double *red);
+
+// ------------------------------------------------------------- batch
+// work description of one instance for the batched pair kernel
+struct co_bwork {
+    const double2 *px, *pg;
+    const double *pw;
+    double *gpart, *apart, *pdot;
+    size_t ld;
+    const co_solver_state *st;
+    int nt, H, nchunk, blk0;
+};
+int co_batch_work_table(co_ctx *const *ctxs, const co_solver_state *const *states, int n,
+                        int W, int KC, co_bwork *tab, int *max_pos);
+int co_pair64_batch(cudaStream_t s, const co_bwork *d_tab, int n, int total, int W, int KC,
+                    int grid, unsigned *d_counter, int max_pos);
 
 // ------------------------------------------------------------- profiling
 // (co_prof.cu) -- event pairs around pair-kernel launches, collected after

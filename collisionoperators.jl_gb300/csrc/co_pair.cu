@@ -492,6 +492,253 @@ k_pair32_sym(const float4 *__restrict__ pfx, const float4 *__restrict__ pfg,
     gp[ST + tid] = ga2;
 }
 
+// ------------------------------------------------------------------ double-single
+//
+// The same symmetric pair sum in double-single arithmetic: every value is an
+// unevaluated sum hi + lo of two FP32 numbers (about 44 significant bits), built
+// from the error-free transformations of Dekker (1971) and Knuth (TAOCP vol. 2):
+// two_sum (6 adds), fast_two_sum (3), two_prod via FMA (2). The intrinsics
+// __fadd_rn/__fsub_rn/__fmul_rn/__fmaf_rn keep the compiler from contracting
+// these sequences. 1/|d| is one Newton step from the MUFU seed. Each ordered
+// pair then costs about 130 FP32 instructions against 11.5 FP64 instructions in
+// k_pair64_sym, i.e. about 5x less issue time on a part whose FP32:FP64 rate is
+// 64:1, at ~1e-13 relative accuracy per term; momentum stays exact to the
+// accumulation round-off because each pair's term is computed once and added
+// with both signs. Used for the FP64 stage of the mixed precision form.
+struct dsf {
+    float h, l;
+};
+
+__device__ __forceinline__ dsf ds_two_sum(float a, float b) {
+    float s = __fadd_rn(a, b);
+    float bb = __fsub_rn(s, a);
+    float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return {s, e};
+}
+__device__ __forceinline__ dsf ds_fast(float a, float b) {
+    float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ dsf ds_add(dsf a, dsf b) {
+    dsf s = ds_two_sum(a.h, b.h);
+    return ds_fast(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ dsf ds_sub(dsf a, dsf b) { return ds_add(a, {-b.h, -b.l}); }
+__device__ __forceinline__ dsf ds_mul(dsf a, dsf b) {
+    float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    return ds_fast(p, e);
+}
+__device__ __forceinline__ dsf ds_mulf(dsf a, float b) {
+    float p = __fmul_rn(a.h, b);
+    float e = __fmaf_rn(a.h, b, -p);
+    e = __fmaf_rn(a.l, b, e);
+    return ds_fast(p, e);
+}
+
+// unweighted pair term u = U(d)(G_a - G_g)/|d| in double-single
+__device__ __forceinline__ void pair_u_ds(const float4 &xg, const float4 &Gg, const float4 &xa,
+                                          const float4 &Ga, dsf &u1, dsf &u2) {
+    dsf d1 = ds_sub({xg.x, xg.z}, {xa.x, xa.z});
+    dsf d2 = ds_sub({xg.y, xg.w}, {xa.y, xa.w});
+    dsf r2 = ds_add(ds_mul(d1, d1), ds_mul(d2, d2));
+    bool ok = r2.h >= 1e-24f;
+    dsf x = ok ? r2 : dsf{1.f, 0.f};
+    float y0 = rsqrtf(x.h);
+    dsf q = ds_mulf(ds_mulf(x, y0), y0);                     // x y0^2 = 1 - e
+    float e = __fsub_rn(__fsub_rn(1.0f, q.h), q.l);
+    dsf y = ds_two_sum(y0, __fmul_rn(__fmul_rn(0.5f, y0), e));  // y0 (1 + e/2)
+    dsf g1 = ds_sub({Ga.x, Ga.z}, {Gg.x, Gg.z});
+    dsf g2 = ds_sub({Ga.y, Ga.w}, {Gg.y, Gg.w});
+    dsf dg = ds_add(ds_mul(d1, g1), ds_mul(d2, g2));
+    dsf cc = ds_mul(dg, ds_mul(y, y));
+    dsf t1 = ds_sub(g1, ds_mul(d1, cc));
+    dsf t2 = ds_sub(g2, ds_mul(d2, cc));
+    if (!ok) y = {0.f, 0.f};
+    u1 = ds_mul(t1, y);
+    u2 = ds_mul(t2, y);
+}
+
+__global__ void __launch_bounds__(ST)
+k_pair_ds_sym(const float4 *__restrict__ pfx, const float4 *__restrict__ pfg,
+              const float *__restrict__ pfw, const float *__restrict__ pfwl, int nt, int H,
+              int KC, double *__restrict__ gpart, double *__restrict__ apart) {
+    __shared__ float4 sx[ST], sg[ST];
+    __shared__ float2 sw[ST];
+    __shared__ float4 sacc[ST];  // {a1.h, a1.l, a2.h, a2.l}
+    const int I = blockIdx.x % nt, chunk = blockIdx.x / nt;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const float4 xg = pfx[I * ST + tid], Gg = pfg[I * ST + tid];
+    const dsf wg = {pfw[I * ST + tid], pfwl[I * ST + tid]};
+    dsf ga1 = {0.f, 0.f}, ga2 = {0.f, 0.f};
+    double gd1 = 0.0, gd2 = 0.0;
+    const int k0 = chunk * KC, k1 = min(H + 1, k0 + KC);
+    for (int k = k0; k < k1; k++) {
+        if (sym_skip(nt, H, I, k)) continue;
+        const int J = (I + k) % nt;
+        __syncthreads();
+        sx[tid] = pfx[J * ST + tid];
+        sg[tid] = pfg[J * ST + tid];
+        sw[tid] = make_float2(pfw[J * ST + tid], pfwl[J * ST + tid]);
+        sacc[tid] = make_float4(0.f, 0.f, 0.f, 0.f);
+        __syncthreads();
+        if (k == 0) {
+            for (int a = 0; a < ST; a++) {
+                dsf u1, u2;
+                pair_u_ds(xg, Gg, sx[a], sg[a], u1, u2);
+                dsf wa = {sw[a].x, sw[a].y};
+                ga1 = ds_add(ga1, ds_mul(wa, u1));
+                ga2 = ds_add(ga2, ds_mul(wa, u2));
+            }
+        } else {
+            for (int r = 0; r < 4; r++) {
+                const int base = ((warp + r) & 3) * 32;
+                float4 a0 = sacc[base + lane];
+                dsf a1 = {a0.x, a0.y}, a2 = {a0.z, a0.w};
+#pragma unroll 2
+                for (int q = 0; q < 32; q++) {
+                    const int ai = base + ((lane + q) & 31);
+                    dsf u1, u2;
+                    pair_u_ds(xg, Gg, sx[ai], sg[ai], u1, u2);
+                    dsf wa = {sw[ai].x, sw[ai].y};
+                    ga1 = ds_add(ga1, ds_mul(wa, u1));
+                    ga2 = ds_add(ga2, ds_mul(wa, u2));
+                    a1 = ds_sub(a1, ds_mul(wg, u1));
+                    a2 = ds_sub(a2, ds_mul(wg, u2));
+                    const int src = (lane + 1) & 31;
+                    a1.h = __shfl_sync(0xffffffffu, a1.h, src);
+                    a1.l = __shfl_sync(0xffffffffu, a1.l, src);
+                    a2.h = __shfl_sync(0xffffffffu, a2.h, src);
+                    a2.l = __shfl_sync(0xffffffffu, a2.l, src);
+                }
+                sacc[base + lane] = make_float4(a1.h, a1.l, a2.h, a2.l);
+                __syncthreads();
+            }
+            double *ap = apart + ((size_t)(k - 1) * nt + J) * 2 * ST;
+            float4 v = sacc[tid];
+            ap[tid] = (double)v.x + (double)v.y;
+            ap[ST + tid] = (double)v.z + (double)v.w;
+        }
+        // fold the tile pair's target-side double-single sum into FP64
+        gd1 += (double)ga1.h + (double)ga1.l;
+        gd2 += (double)ga2.h + (double)ga2.l;
+        ga1 = {0.f, 0.f};
+        ga2 = {0.f, 0.f};
+    }
+    double *gp = gpart + ((size_t)chunk * nt + I) * 2 * ST;
+    gp[tid] = gd1;
+    gp[ST + tid] = gd2;
+}
+
+// Symmetric FP32 metric: U(d) = (I - d d^T/|d|^2)/|d| is even in d, so one
+// evaluation adds w_a U to A_g and w_g U to A_a (same tiling and rotation as
+// k_pair32_sym; head+tail differences). Partials: 3 components.
+__device__ __forceinline__ void metric_u32(const float4 &xg, const float4 &xa, float &u11,
+                                           float &u12, float &u22) {
+    float d1 = (xg.x - xa.x) + (xg.z - xa.z);
+    float d2 = (xg.y - xa.y) + (xg.w - xa.w);
+    float q11 = d1 * d1, q22 = d2 * d2;
+    float r2 = q11 + q22;
+    float y = rsqrtf(r2);
+    y = r2 >= 1e-24f ? y : 0.0f;
+    float y2 = y * y;
+    u11 = y * fmaf(-q11, y2, 1.f);
+    u12 = -y * (d1 * d2 * y2);
+    u22 = y * fmaf(-q22, y2, 1.f);
+}
+
+__global__ void __launch_bounds__(ST)
+k_metric32_sym(const float4 *__restrict__ pfx, const float *__restrict__ pfw, int nt, int H,
+               int KC, double *__restrict__ gpart, float *__restrict__ apart) {
+    __shared__ float4 sx[ST];
+    __shared__ float sw[ST];
+    __shared__ float4 sacc[ST];
+    const int I = blockIdx.x % nt, chunk = blockIdx.x / nt;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const float4 xg = pfx[I * ST + tid];
+    const float wg = pfw[I * ST + tid];
+    double g11 = 0.0, g12 = 0.0, g22 = 0.0;
+    const int k0 = chunk * KC, k1 = min(H + 1, k0 + KC);
+    for (int k = k0; k < k1; k++) {
+        if (sym_skip(nt, H, I, k)) continue;
+        const int J = (I + k) % nt;
+        __syncthreads();
+        sx[tid] = pfx[J * ST + tid];
+        sw[tid] = pfw[J * ST + tid];
+        sacc[tid] = make_float4(0.f, 0.f, 0.f, 0.f);
+        __syncthreads();
+        float t11 = 0.f, t12 = 0.f, t22 = 0.f;
+        if (k == 0) {
+#pragma unroll 8
+            for (int a = 0; a < ST; a++) {
+                float u11, u12, u22;
+                metric_u32(xg, sx[a], u11, u12, u22);
+                t11 = fmaf(sw[a], u11, t11);
+                t12 = fmaf(sw[a], u12, t12);
+                t22 = fmaf(sw[a], u22, t22);
+            }
+        } else {
+            for (int r = 0; r < 4; r++) {
+                const int base = ((warp + r) & 3) * 32;
+                float4 a0 = sacc[base + lane];
+                float a11 = a0.x, a12 = a0.y, a22 = a0.z;
+#pragma unroll 8
+                for (int q = 0; q < 32; q++) {
+                    const int ai = base + ((lane + q) & 31);
+                    float u11, u12, u22;
+                    metric_u32(xg, sx[ai], u11, u12, u22);
+                    const float wa = sw[ai];
+                    t11 = fmaf(wa, u11, t11);
+                    t12 = fmaf(wa, u12, t12);
+                    t22 = fmaf(wa, u22, t22);
+                    a11 = fmaf(wg, u11, a11);
+                    a12 = fmaf(wg, u12, a12);
+                    a22 = fmaf(wg, u22, a22);
+                    const int src = (lane + 1) & 31;
+                    a11 = __shfl_sync(0xffffffffu, a11, src);
+                    a12 = __shfl_sync(0xffffffffu, a12, src);
+                    a22 = __shfl_sync(0xffffffffu, a22, src);
+                }
+                sacc[base + lane] = make_float4(a11, a12, a22, 0.f);
+                __syncthreads();
+            }
+            float *ap = apart + ((size_t)(k - 1) * nt + J) * 3 * ST;
+            float4 v = sacc[tid];
+            ap[tid] = v.x;
+            ap[ST + tid] = v.y;
+            ap[2 * ST + tid] = v.z;
+        }
+        g11 += (double)t11;
+        g12 += (double)t12;
+        g22 += (double)t22;
+    }
+    double *gp = gpart + ((size_t)chunk * nt + I) * 3 * ST;
+    gp[tid] = g11;
+    gp[ST + tid] = g12;
+    gp[2 * ST + tid] = g22;
+}
+
+__global__ void k_metric_reduce(const double *__restrict__ gpart, const float *__restrict__ apart,
+                                int nt, int H, int nchunk, double *__restrict__ dst, size_t ld) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nt * ST) return;
+    int K = p / ST, t = p - K * ST;
+    double s[3] = {0.0, 0.0, 0.0};
+    for (int c = 0; c < nchunk; c++) {
+        const double *gp = gpart + ((size_t)c * nt + K) * 3 * ST;
+        for (int q = 0; q < 3; q++) s[q] += gp[q * ST + t];
+    }
+    for (int k = 1; k <= H; k++) {
+        int I = (K - k + nt) % nt;
+        if (sym_skip(nt, H, I, k)) continue;
+        const float *ap = apart + ((size_t)(k - 1) * nt + K) * 3 * ST;
+        for (int q = 0; q < 3; q++) s[q] += (double)ap[q * ST + t];
+    }
+    for (int q = 0; q < 3; q++) dst[(size_t)q * ld + p] = s[q];
+}
+
 // vdot[p] = sum over chunks of the target-side partials + sum over k of the
 // source-side partials, in that fixed order
 template <typename TA>
@@ -538,19 +785,20 @@ __global__ void k_pack_landau(const int *__restrict__ perm, const int *__restric
                               const double *__restrict__ vmid, const double *__restrict__ dS,
                               const double *__restrict__ dv, const double *__restrict__ w,
                               const co_solver_state *__restrict__ st, int use_lambda,
-                              int precision, double2 *__restrict__ px, double2 *__restrict__ pg,
+                              int mode, double2 *__restrict__ px, double2 *__restrict__ pg,
                               double *__restrict__ pw, float4 *__restrict__ pfx,
-                              float4 *__restrict__ pfg, float *__restrict__ pfw) {
+                              float4 *__restrict__ pfg, float *__restrict__ pfw, float *__restrict__ pfwl) {
     int M = *Mp;
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= Mpad) return;
     if (p >= M) {  // inert padding up to the tile boundary: far away, zero weight
-        if (precision != CO_PREC_FP64) {
+        if (mode & 2) {
             pfx[p] = make_float4(1e3f, 1e3f, 0.f, 0.f);
             pfg[p] = make_float4(0.f, 0.f, 0.f, 0.f);
             pfw[p] = 0.f;
+            pfwl[p] = 0.f;
         }
-        if (precision != CO_PREC_MIXED) {
+        if (mode & 1) {
             px[p] = make_double2(1e3, 1e3);
             pg[p] = make_double2(0.0, 0.0);
             pw[p] = 0.0;
@@ -563,13 +811,15 @@ __global__ void k_pack_landau(const int *__restrict__ perm, const int *__restric
     double x1 = vmid[a], x2 = vmid[N + a];
     double G1 = -(dS[a] + lam * dv[a]) * iw;
     double G2 = -(dS[N + a] + lam * dv[N + a]) * iw;
-    if (precision != CO_PREC_FP64) {
+    if (mode & 2) {
         float x1h = (float)x1, x2h = (float)x2, G1h = (float)G1, G2h = (float)G2;
         pfx[p] = make_float4(x1h, x2h, (float)(x1 - (double)x1h), (float)(x2 - (double)x2h));
         pfg[p] = make_float4(G1h, G2h, (float)(G1 - (double)G1h), (float)(G2 - (double)G2h));
-        pfw[p] = (float)w[a];
+        float wh = (float)w[a];
+        pfw[p] = wh;
+        pfwl[p] = (float)(w[a] - (double)wh);
     }
-    if (precision != CO_PREC_MIXED) {
+    if (mode & 1) {
         px[p] = make_double2(x1, x2);
         pg[p] = make_double2(G1, G2);
         pw[p] = w[a];
@@ -579,20 +829,21 @@ __global__ void k_pack_landau(const int *__restrict__ perm, const int *__restric
 // Hook pack: operands straight from (v, G, w) (COLLISION_FN semantics).
 __global__ void k_pack_plain(const int *__restrict__ perm, const int *__restrict__ Mp, int Mpad, int N,
                              const double *__restrict__ v, const double *__restrict__ G,
-                             const double *__restrict__ w, int precision,
+                             const double *__restrict__ w, int mode,
                              double2 *__restrict__ px, double2 *__restrict__ pg,
                              double *__restrict__ pw, float4 *__restrict__ pfx,
-                             float4 *__restrict__ pfg, float *__restrict__ pfw) {
+                             float4 *__restrict__ pfg, float *__restrict__ pfw, float *__restrict__ pfwl) {
     int M = *Mp;
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= Mpad) return;
     if (p >= M) {  // inert padding up to the tile boundary: far away, zero weight
-        if (precision != CO_PREC_FP64) {
+        if (mode & 2) {
             pfx[p] = make_float4(1e3f, 1e3f, 0.f, 0.f);
             pfg[p] = make_float4(0.f, 0.f, 0.f, 0.f);
             pfw[p] = 0.f;
+            pfwl[p] = 0.f;
         }
-        if (precision != CO_PREC_MIXED) {
+        if (mode & 1) {
             px[p] = make_double2(1e3, 1e3);
             pg[p] = make_double2(0.0, 0.0);
             pw[p] = 0.0;
@@ -601,13 +852,15 @@ __global__ void k_pack_plain(const int *__restrict__ perm, const int *__restrict
     }
     int a = perm[p];
     double x1 = v[a], x2 = v[N + a], G1 = G[a], G2 = G[N + a];
-    if (precision != CO_PREC_FP64) {
+    if (mode & 2) {
         float x1h = (float)x1, x2h = (float)x2, G1h = (float)G1, G2h = (float)G2;
         pfx[p] = make_float4(x1h, x2h, (float)(x1 - (double)x1h), (float)(x2 - (double)x2h));
         pfg[p] = make_float4(G1h, G2h, (float)(G1 - (double)G1h), (float)(G2 - (double)G2h));
-        pfw[p] = (float)w[a];
+        float wh = (float)w[a];
+        pfw[p] = wh;
+        pfwl[p] = (float)(w[a] - (double)wh);
     }
-    if (precision != CO_PREC_MIXED) {
+    if (mode & 1) {
         px[p] = make_double2(x1, x2);
         pg[p] = make_double2(G1, G2);
         pw[p] = w[a];
@@ -738,8 +991,10 @@ int co_pair_fp64(co_ctx *c, int Mub, int with_metric) {
 
 #define SYM_KC 8
 
-// symmetric pair sum on the padded operands (Mpad = nt * ST)
-static int pair_sym(co_ctx *c, int Mub, int fp64) {
+// symmetric pair sum on the padded operands (Mpad = nt * ST);
+// kind: 0 FP32, 1 FP64, 2 double-single
+static int pair_sym(co_ctx *c, int Mub, int kind) {
+    const int fp64 = kind != 0;  // partials of the source side in double
     int nt = co_cdiv(Mub, ST);
     int H = nt / 2;
     int KC = SYM_KC;
@@ -750,8 +1005,15 @@ static int pair_sym(co_ctx *c, int Mub, int fp64) {
     int rc = ensure_part(c, need);
     if (rc) return rc;
     double *gpart = c->mb.part;
-    co_prof_begin(c, fp64);
-    if (fp64) {
+    co_prof_begin(c, kind == 1 ? 1 : (kind == 2 ? 2 : 0));
+    if (kind == 2) {
+        double *apart = c->mb.part + gsz;
+        k_pair_ds_sym<<<nt * nchunk, ST, 0, c->stream>>>(c->mb.pf_x, c->mb.pf_g, c->mb.pf_w,
+                                                         c->mb.pf_wl, nt, H, KC, gpart, apart);
+        co_prof_end(c);
+        k_sym_reduce<double><<<co_cdiv((long long)nt * ST, 256), 256, 0, c->stream>>>(
+            gpart, apart, nt, H, nchunk, c->mb.pdot, (size_t)c->mb.cap);
+    } else if (fp64) {
         double *apart = c->mb.part + gsz;
         k_pair64_sym<<<nt * nchunk, ST, 0, c->stream>>>(c->mb.px, c->mb.pg, c->mb.pw, nt, H, KC,
                                                         gpart, apart);
@@ -806,10 +1068,10 @@ int co_pack_plain(co_ctx *c, int N, int Mub, int precision, const double *x, con
     if (Mub <= 0) return CO_OK;
     const int *Mp = c->mb.cstart + c->n_el;
     co_bufs &b = c->mb;
-    int Mpad = co_cdiv(Mub, PAIR_TPB) * PAIR_TPB;
-    k_pack_plain<<<co_cdiv(Mpad, 256), 256, 0, c->stream>>>(b.perm, Mp, Mpad, N, x, G, b.w, precision,
-                                                           b.px, b.pg, b.pw, b.pf_x, b.pf_g,
-                                                           b.pf_w);
+    int Mpad = co_cdiv(Mub, 256) * 256;  // whole tiles of up to 256 markers
+    k_pack_plain<<<co_cdiv(Mpad, 256), 256, 0, c->stream>>>(b.perm, Mp, Mpad, N, x, G, b.w,
+                                                            co_pack_mode(precision), b.px, b.pg,
+                                                            b.pw, b.pf_x, b.pf_g, b.pf_w, b.pf_wl);
     c->launches++;
     CO_CK(cudaGetLastError());
     return CO_OK;
@@ -819,10 +1081,10 @@ int co_pack_landau(co_ctx *c, int N, int Mub, int precision, int gonzalez) {
     if (Mub <= 0) return CO_OK;
     const int *Mp = c->mb.cstart + c->n_el;
     co_bufs &b = c->mb;
-    int Mpad = co_cdiv(Mub, PAIR_TPB) * PAIR_TPB;
+    int Mpad = co_cdiv(Mub, 256) * 256;  // whole tiles of up to 256 markers
     k_pack_landau<<<co_cdiv(Mpad, 256), 256, 0, c->stream>>>(
-        b.perm, Mp, Mpad, N, b.vmid, b.dS, b.dv, b.w, c->st, gonzalez, precision, b.px, b.pg, b.pw,
-        b.pf_x, b.pf_g, b.pf_w);
+        b.perm, Mp, Mpad, N, b.vmid, b.dS, b.dv, b.w, c->st, gonzalez, co_pack_mode(precision),
+        b.px, b.pg, b.pw, b.pf_x, b.pf_g, b.pf_w, b.pf_wl);
     c->launches++;
     CO_CK(cudaGetLastError());
     return CO_OK;
@@ -852,10 +1114,201 @@ int co_unpack_A(co_ctx *c, int N, double *A) {
 
 int co_metric32(co_ctx *c, int Mub) {
     if (Mub <= 0) return CO_OK;
+    if (c->pair_symmetric && co_cdiv(Mub, ST) >= 4) {
+        int nt = co_cdiv(Mub, ST), H = nt / 2, KC = SYM_KC, nchunk = co_cdiv(H + 1, KC);
+        size_t gsz = (size_t)nchunk * nt * 3 * ST;
+        size_t asz = (size_t)(H > 0 ? H : 1) * nt * 3 * ST;  // floats
+        int rc = ensure_part(c, gsz + (asz + 1) / 2);
+        if (rc) return rc;
+        float *apart = (float *)(c->mb.part + gsz);
+        k_metric32_sym<<<nt * nchunk, ST, 0, c->stream>>>(c->mb.pf_x, c->mb.pf_w, nt, H, KC,
+                                                          c->mb.part, apart);
+        k_metric_reduce<<<co_cdiv((long long)nt * ST, 256), 256, 0, c->stream>>>(
+            c->mb.part, apart, nt, H, nchunk, c->mb.pA, (size_t)c->mb.cap);
+        c->launches += 2;
+        CO_CK(cudaGetLastError());
+        return CO_OK;
+    }
     const int *Mp = c->mb.cstart + c->n_el;
     k_metric32<<<co_cdiv(Mub, PAIR_TPB), PAIR_TPB, 0, c->stream>>>(c->mb.pf_x, c->mb.pf_w, Mp,
                                                                    c->mb.pA, (size_t)c->mb.cap);
     c->launches++;
+    CO_CK(cudaGetLastError());
+    return CO_OK;
+}
+
+// FP64-equivalent pair sum in double-single arithmetic (symmetric kernel);
+// falls back to the FP64 kernel below 4 tiles
+int co_pair_ds(co_ctx *c, int Mub) {
+    if (Mub <= 0) return CO_OK;
+    if (co_cdiv(Mub, ST) >= 4) return pair_sym(c, Mub, 2);
+    return co_pair_fp64(c, Mub, 0);
+}
+
+// ================================================================== batched
+//
+// Many independent ensembles in one persistent launch: the work items of all
+// Landau instances -- (instance, tile I, chunk of k) as in k_pair64_sym, with a
+// tile of T = 32 W markers -- are handed out through an atomic counter, so the
+// grid size and the tile shape are free parameters (chosen by the autotuner of
+// the batch engine). Items of instances whose solve has finished are skipped.
+// Every item writes its own partial slots, so the result does not depend on
+// which block ran which item.
+template <int W>
+__global__ void __launch_bounds__(32 * W)
+k_pair64_sym_batch(const co_bwork *__restrict__ works, int n_inst, int total, int KC,
+                   unsigned *__restrict__ counter) {
+    constexpr int T = 32 * W;
+    __shared__ double2 sx[T], sg[T];
+    __shared__ double sw[T];
+    __shared__ double2 sacc[T];
+    __shared__ int s_item;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (;;) {
+        if (tid == 0) s_item = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int item = s_item;
+        __syncthreads();
+        if (item >= total) return;
+        int lo = 0, hi = n_inst;
+        while (hi - lo > 1) {
+            int mid = (lo + hi) >> 1;
+            if (works[mid].blk0 <= item) lo = mid; else hi = mid;
+        }
+        const co_bwork wk = works[lo];
+        if (wk.st->done) continue;
+        const int b = item - wk.blk0;
+        const int nt = wk.nt, H = wk.H;
+        const int I = b % nt, chunk = b / nt;
+        const double2 xg = wk.px[I * T + tid], Gg = wk.pg[I * T + tid];
+        const double wg = wk.pw[I * T + tid];
+        double ga1 = 0.0, ga2 = 0.0;
+        const int k0 = chunk * KC, k1 = min(H + 1, k0 + KC);
+        for (int k = k0; k < k1; k++) {
+            if (sym_skip(nt, H, I, k)) continue;
+            const int J = (I + k) % nt;
+            __syncthreads();
+            sx[tid] = wk.px[J * T + tid];
+            sg[tid] = wk.pg[J * T + tid];
+            sw[tid] = wk.pw[J * T + tid];
+            sacc[tid] = make_double2(0.0, 0.0);
+            __syncthreads();
+            if (k == 0) {
+#pragma unroll 4
+                for (int a = 0; a < T; a++) {
+                    double u1, u2;
+                    double2 xa = sx[a], Ga = sg[a];
+                    pair_u64(xg.x - xa.x, xg.y - xa.y, Ga.x - Gg.x, Ga.y - Gg.y, u1, u2);
+                    ga1 = fma(sw[a], u1, ga1);
+                    ga2 = fma(sw[a], u2, ga2);
+                }
+                continue;
+            }
+            for (int r = 0; r < W; r++) {
+                const int base = ((warp + r) % W) * 32;
+                double2 a0 = sacc[base + lane];
+                double a1 = a0.x, a2 = a0.y;
+#pragma unroll 4
+                for (int q = 0; q < 32; q++) {
+                    const int ai = base + ((lane + q) & 31);
+                    double2 xa = sx[ai], Ga = sg[ai];
+                    double wa = sw[ai];
+                    double u1, u2;
+                    pair_u64(xg.x - xa.x, xg.y - xa.y, Ga.x - Gg.x, Ga.y - Gg.y, u1, u2);
+                    ga1 = fma(wa, u1, ga1);
+                    ga2 = fma(wa, u2, ga2);
+                    a1 = fma(-wg, u1, a1);
+                    a2 = fma(-wg, u2, a2);
+                    a1 = __shfl_sync(0xffffffffu, a1, (lane + 1) & 31);
+                    a2 = __shfl_sync(0xffffffffu, a2, (lane + 1) & 31);
+                }
+                sacc[base + lane] = make_double2(a1, a2);
+                __syncthreads();
+            }
+            double *ap = wk.apart + ((size_t)(k - 1) * nt + J) * 2 * T;
+            ap[tid] = sacc[tid].x;
+            ap[T + tid] = sacc[tid].y;
+        }
+        double *gp = wk.gpart + ((size_t)chunk * nt + I) * 2 * T;
+        gp[tid] = ga1;
+        gp[T + tid] = ga2;
+    }
+}
+
+// fixed-order reduction of every instance's partials (blockIdx.y = instance)
+__global__ void k_sym_reduce_batch(const co_bwork *__restrict__ works, int T) {
+    const co_bwork wk = works[blockIdx.y];
+    if (wk.st->done) return;
+    const int nt = wk.nt, H = wk.H;
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nt * T) return;
+    int K = p / T, t = p - K * T;
+    double s1 = 0.0, s2 = 0.0;
+    for (int c = 0; c < wk.nchunk; c++) {
+        const double *gp = wk.gpart + ((size_t)c * nt + K) * 2 * T;
+        s1 += gp[t];
+        s2 += gp[T + t];
+    }
+    for (int k = 1; k <= H; k++) {
+        int I = (K - k + nt) % nt;
+        if (sym_skip(nt, H, I, k)) continue;
+        const double *ap = wk.apart + ((size_t)(k - 1) * nt + K) * 2 * T;
+        s1 += ap[t];
+        s2 += ap[T + t];
+    }
+    wk.pdot[p] = s1;
+    wk.pdot[wk.ld + p] = s2;
+}
+
+// Fill the work table of a batch for tile width T = 32 W and chunk KC; makes
+// sure every instance's partial buffer is large enough. Returns the number of
+// work items.
+int co_batch_work_table(co_ctx *const *ctxs, const co_solver_state *const *states, int n,
+                        int W, int KC, co_bwork *tab, int *max_pos) {
+    const int T = 32 * W;
+    int blk = 0, mp = 0;
+    for (int i = 0; i < n; i++) {
+        co_ctx *c = ctxs[i];
+        co_bwork &wk = tab[i];
+        int N = c->batch_N;
+        int nt = co_cdiv(N, T), H = nt / 2, nchunk = co_cdiv(H + 1, KC);
+        size_t gsz = (size_t)nchunk * nt * 2 * T, asz = (size_t)(H > 0 ? H : 1) * nt * 2 * T;
+        if (c->batch_landau) {
+            int rc = ensure_part(c, gsz + asz);
+            if (rc) return -rc;
+        }
+        wk.px = c->mb.px;
+        wk.pg = c->mb.pg;
+        wk.pw = c->mb.pw;
+        wk.gpart = c->mb.part;
+        wk.apart = c->mb.part + gsz;
+        wk.pdot = c->mb.pdot;
+        wk.ld = (size_t)c->mb.cap;
+        wk.st = states[i];
+        wk.nt = c->batch_landau ? nt : 0;   // LB instances have no pair sum
+        wk.H = H;
+        wk.nchunk = nchunk;
+        wk.blk0 = blk;
+        blk += c->batch_landau ? nt * nchunk : 0;
+        if (c->batch_landau && nt * T > mp) mp = nt * T;
+    }
+    *max_pos = mp;
+    return blk;
+}
+
+// one batched symmetric FP64 pair sum over all Landau instances
+int co_pair64_batch(cudaStream_t s, const co_bwork *d_tab, int n, int total, int W, int KC,
+                    int grid, unsigned *d_counter, int max_pos) {
+    if (total <= 0) return CO_OK;
+    CO_CK(cudaMemsetAsync(d_counter, 0, sizeof(unsigned), s));
+    switch (W) {
+        case 2: k_pair64_sym_batch<2><<<grid, 64, 0, s>>>(d_tab, n, total, KC, d_counter); break;
+        case 4: k_pair64_sym_batch<4><<<grid, 128, 0, s>>>(d_tab, n, total, KC, d_counter); break;
+        case 8: k_pair64_sym_batch<8><<<grid, 256, 0, s>>>(d_tab, n, total, KC, d_counter); break;
+        default: return CO_ERR_ARG;
+    }
+    dim3 rg(co_cdiv(max_pos, 256), n);
+    k_sym_reduce_batch<<<rg, 256, 0, s>>>(d_tab, 32 * W);
     CO_CK(cudaGetLastError());
     return CO_OK;
 }

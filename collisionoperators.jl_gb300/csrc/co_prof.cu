@@ -41,7 +41,11 @@ void co_prof_collect(co_ctx *c) {
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, e.a, e.b) != cudaSuccess) continue;
         double M = (double)p->Mpinned[e.slot];
-        if (e.fp64) {
+        if (e.fp64 == 2) {
+            p->acc.pairds_ms += ms;
+            p->acc.pairds_launches++;
+            p->acc.pairds_pairs += M * (M - 1.0);
+        } else if (e.fp64) {
             p->acc.pair64_ms += ms;
             p->acc.pair64_launches++;
             p->acc.pair64_pairs += M * (M - 1.0);
@@ -102,7 +106,7 @@ extern "C" int co_profile(co_ctx *c, int enable) {
             CO_CK(cudaMallocHost(&p->Mpinned, sizeof(int) * CO_PROF_POOL));
         }
         memset(&p->acc, 0, sizeof(p->acc));
-        c->maps32 = c->maps64 = 0;
+        c->maps32 = c->maps64 = c->mapsds = 0;
     }
     p->on = enable ? 1 : 0;
     return CO_OK;
@@ -117,6 +121,7 @@ extern "C" int co_profile_read(co_ctx *c, co_profile_t *out) {
     *out = p->acc;
     out->maps64 = c->maps64;
     out->maps32 = c->maps32;
+    out->mapsds = c->mapsds;
     return CO_OK;
 }
 

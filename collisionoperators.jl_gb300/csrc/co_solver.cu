@@ -19,6 +19,8 @@
 #include "co_internal.cuh"
 #include "co_reduce.cuh"
 
+#include <vector>
+
 #define CO_RED_COMPS 16
 #define CO_BARRIER_SPINS (1 << 22)
 
@@ -164,6 +166,89 @@ k_lb_fused(int N, const double *__restrict__ vmid, const double *__restrict__ w,
     }
 }
 
+// The same LB drift in two launches without a grid barrier (for CUDA-graph
+// capture in the batch engine): pass 1 applies lambda and writes the block
+// partials of the seven moments; pass 2 reduces them redundantly in every
+// block in the same fixed order, solves the 3x3 system and writes the drift.
+__global__ void __launch_bounds__(CO_RED_THREADS)
+k_lb_part(int N, const double *__restrict__ vmid, const double *__restrict__ w,
+          double *__restrict__ g, const double *__restrict__ dv, int use_lambda,
+          const co_solver_state *st, double *__restrict__ red7) {
+    __shared__ double sh[32];
+    const double lam = use_lambda ? st->lambda : 0.0;
+    double m[7] = {0, 0, 0, 0, 0, 0, 0};
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < N; a += gridDim.x * blockDim.x) {
+        double wa = w[a], x = vmid[a], y = vmid[N + a];
+        double g1 = g[a], g2 = g[N + a];
+        if (use_lambda) {
+            double iw = 1.0 / wa;
+            g1 -= lam * dv[a] * iw;
+            g2 -= lam * dv[N + a] * iw;
+            g[a] = g1;
+            g[N + a] = g2;
+        }
+        m[0] += wa;
+        m[1] += wa * x;
+        m[2] += wa * y;
+        m[3] += wa * (x * x + y * y);
+        m[4] += wa * g1;
+        m[5] += wa * g2;
+        m[6] += wa * (x * g1 + y * g2);
+    }
+    for (int k = 0; k < 7; k++) {
+        double s = co_block_sum(m[k], sh);
+        if (threadIdx.x == 0) red7[blockIdx.x * 8 + k] = s;
+    }
+}
+
+__global__ void __launch_bounds__(CO_RED_THREADS)
+k_lb_apply(int N, int nred7, const double *__restrict__ red7, const double *__restrict__ vmid,
+           const double *__restrict__ g, double nu, double dt, const double *__restrict__ v0,
+           double *__restrict__ Gv, const double *__restrict__ v1, double *__restrict__ r,
+           double *__restrict__ red2, co_solver_state *st) {
+    __shared__ double sh[32];
+    __shared__ double sol[3];
+    double tot[7];
+    for (int k = 0; k < 7; k++) tot[k] = co_sum_partials(red7, nred7, 8, k, sh);
+    if (threadIdx.x == 0) {
+        double M[9] = {tot[0], 0.0, tot[1], 0.0, tot[0], tot[2], tot[1], tot[2], tot[3]};
+        double b[3] = {-tot[4], -tot[5], -tot[6]};
+        lu3_solve(M, b);
+        sol[0] = b[0]; sol[1] = b[1]; sol[2] = b[2];
+        if (blockIdx.x == 0) {
+            for (int k = 0; k < 7; k++) st->lb[k] = tot[k];
+            st->ab[0] = b[0]; st->ab[1] = b[1]; st->ab[2] = b[2];
+        }
+    }
+    __syncthreads();
+    const double A1 = sol[0], A2 = sol[1], B = sol[2];
+    double sr = 0.0, sv = 0.0;
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < N; a += gridDim.x * blockDim.x) {
+        double x = vmid[a], y = vmid[N + a];
+        double q1 = -nu * (g[a] + A1 + B * x);
+        double q2 = -nu * (g[N + a] + A2 + B * y);
+        double o1 = v0[a] + dt * q1, o2 = v0[N + a] + dt * q2;
+        Gv[a] = o1;
+        Gv[N + a] = o2;
+        if (r) {
+            double x1 = v1[a], x2 = v1[N + a];
+            double r1 = o1 - x1, r2 = o2 - x2;
+            r[a] = r1;
+            r[N + a] = r2;
+            sr += r1 * r1 + r2 * r2;
+            sv += x1 * x1 + x2 * x2;
+        }
+    }
+    if (r) {
+        double s1 = co_block_sum(sr, sh);
+        double s2 = co_block_sum(sv, sh);
+        if (threadIdx.x == 0) {
+            red2[blockIdx.x * 2 + 0] = s1;
+            red2[blockIdx.x * 2 + 1] = s2;
+        }
+    }
+}
+
 // ---------------------------------------------------------------- Anderson
 
 struct co_dev_opts {
@@ -178,6 +263,7 @@ __global__ void k_state_reset(co_solver_state *st) {
         st->slot = 0;
         st->n_restart = 0;
         st->k64 = 0;
+        st->finished = 0;
         st->done = 0;
         st->path = 0;
         st->improved = 0;
@@ -496,6 +582,18 @@ static int picard_map_impl(co_ctx *c, int model, int gonzalez, double nu, int pr
         k_lambda<<<1, 256, 0, c->stream>>>(b.red, nred, c->st, S0, gonzalez);
         c->launches++;
         CO_CK(cudaGetLastError());
+        if (c->lb_two_pass) {
+            int g1 = nred;  // grid of both passes
+            double *red7 = b.red + (size_t)b.red_cap * 8;
+            k_lb_part<<<g1, CO_RED_THREADS, 0, c->stream>>>(N, b.vmid, b.w, b.G, b.dv, gonzalez,
+                                                           c->st, red7);
+            k_lb_apply<<<g1, CO_RED_THREADS, 0, c->stream>>>(N, g1, red7, b.vmid, b.G, nu, dt, v0,
+                                                            Gv, vin, r, b.red, c->st);
+            c->launches += 2;
+            CO_CK(cudaGetLastError());
+            if (nred_out) *nred_out = g1;
+            return CO_OK;
+        }
         if ((rc = co_lb_fused(c, N, nu, dt, Gv, v0, b.vmid, b.w, b.G, b.dv, gonzalez, vin, r)))
             return rc;
         // residual partials of the fused kernel use its own grid size
@@ -512,6 +610,9 @@ static int picard_map_impl(co_ctx *c, int model, int gonzalez, double nu, int pr
         if (precision == CO_PREC_MIXED) {
             rc = co_pair_fp32(c, N);
             c->maps32++;
+        } else if (precision == CO_PREC_MIXED_DS) {
+            rc = co_pair_ds(c, N);
+            c->mapsds++;
         } else {
             rc = co_pair_fp64(c, N, 0);
             c->maps64++;
@@ -614,17 +715,18 @@ int co_step_anderson_buffers(co_ctx *c, const co_opts *o, int N, double S0, doub
         return CO_OK;
     }
     int it = 0;
-    if (o->precision == CO_PREC_MIXED) {
+    if (o->precision == CO_PREC_MIXED || o->precision == CO_PREC_MIXED_DS) {
         // phase 1: Anderson on the FP32-pair map, floored at mixed_floor
         double fl = o->mixed_floor > 0 ? o->mixed_floor : 0.0;
         co_dev_opts d = dev_opts(o, fl);
         if ((rc = anderson_loop(c, o, CO_PREC_MIXED, N, S0, dt, d, o->max_iter, &it))) return rc;
         double r0_32 = c->st_host->nrm_r0;
         int nrs32 = c->st_host->n_restart;
-        // phase 2: the FP64 exit Picard map G64(v) (exit_picard_step)
+        // phase 2: the FP64 (or double-single) exit Picard map (exit_picard_step)
         co_bufs &b = c->mb;
         int nred = 0;
-        if ((rc = picard_map_impl(c, o->model, o->use_gonzalez, o->nu, CO_PREC_FP64, b.Gv, b.v1,
+        int exit_prec = o->precision == CO_PREC_MIXED_DS ? CO_PREC_MIXED_DS : CO_PREC_FP64;
+        if ((rc = picard_map_impl(c, o->model, o->use_gonzalez, o->nu, exit_prec, b.Gv, b.v1,
                                   b.v0, N, S0, dt, b.r, &nred)))
             return rc;
         co_dev_opts d64 = dev_opts(o, 0.0);
@@ -672,8 +774,10 @@ int co_predictor_buffers(co_ctx *c, const co_opts *o, int precision, const doubl
         if ((rc = co_compute_r_dev(c, c->f, c->rr))) return rc;
         if ((rc = co_mass_solve_dev(c, c->rr, c->L))) return rc;
         if ((rc = co_grad_L_dev(c, v, N, c->L, b.G, nullptr, nullptr, nullptr, nullptr))) return rc;
-        if ((rc = co_pack_plain(c, N, N, precision, v, b.G))) return rc;
-        rc = precision == CO_PREC_MIXED ? co_pair_fp32(c, N) : co_pair_fp64(c, N, 0);
+        // the predictor is an initial guess: the mixed forms take the FP32 pair sum
+        const int pprec = precision == CO_PREC_FP64 ? CO_PREC_FP64 : CO_PREC_MIXED;
+        if ((rc = co_pack_plain(c, N, N, pprec, v, b.G))) return rc;
+        rc = pprec == CO_PREC_MIXED ? co_pair_fp32(c, N) : co_pair_fp64(c, N, 0);
         if (rc) return rc;
         if ((rc = co_unpack_update(c, N, dt, out, v, nullptr, nullptr, nullptr))) return rc;
     }
@@ -885,7 +989,8 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
     d.stag_window = dopt->stag_window;
     d.fp32_stall = dopt->fp32_stall > 0 ? dopt->fp32_stall : 0.5;
     co_dev_opts di = dev_opts(o, 0.0);
-    int stage = o->precision == CO_PREC_MIXED ? 1 : 0;
+    int stage = o->precision != CO_PREC_FP64 ? 1 : 0;
+    const int ds = o->precision == CO_PREC_MIXED_DS;  // FP64 stage in double-single
     int max_outer = o->max_iter;
     int total_inner = 0;
     k_state_reset<<<1, 32, 0, c->stream>>>(c->st);
@@ -896,12 +1001,15 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
         if ((rc = landau_geff_dev(c, gz, b.v1, b.v0, N, S0))) return rc;
         k_geff_store<<<co_cdiv(N, 256), 256, 0, c->stream>>>(N, b.dS, b.dv, b.w, c->st, gz, b.Gk);
         c->launches++;
-        const int m64 = dopt->metric64 && stage == 0;
-        int prec_pack = stage == 1 ? CO_PREC_MIXED : (m64 ? CO_PREC_FP64 : CO_PREC_BOTH);
+        const int m64 = dopt->metric64 && stage == 0 && !ds;
+        int prec_pack = (stage == 1 || ds) ? CO_PREC_MIXED : (m64 ? CO_PREC_FP64 : CO_PREC_BOTH);
         if ((rc = co_pack_landau(c, N, N, prec_pack, gz))) return rc;
         if (stage == 1) {
             rc = co_pair_fp32(c, N);
             c->maps32++;
+        } else if (ds) {
+            rc = co_pair_ds(c, N);
+            c->mapsds++;
         } else {
             rc = co_pair_fp64(c, N, m64);   // with_metric: F and A in one FP64 pass
             c->maps64++;
@@ -971,4 +1079,492 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
     if (inner) *inner = total_inner;
     if (r0) *r0 = c->st_host->nrm_r0;
     return CO_OK;
+}
+
+// ================================================================ batch engine
+//
+// Many independent ensembles (Landau or LB, different N and meshes) advance
+// together: one context per instance, all on one stream; per Picard iteration
+// every instance's O(N) stage, ONE persistent launch of the batched symmetric
+// FP64 pair kernel for all Landau instances, and every instance's Anderson
+// control. The iteration is captured once per time step as a CUDA graph and
+// replayed until every instance has exited; converged instances are skipped by
+// the pair kernel and their state no longer changes. Tile width, chunk size and
+// grid size of the pair kernel are chosen by timing candidates on the batch's
+// own data (co_batch_tune).
+
+struct co_batch {
+    int device;
+    cudaStream_t stream;
+    int n;
+    std::vector<co_ctx *> ctx;
+    std::vector<int> N, model;
+    std::vector<double> nu;
+    std::vector<size_t> off;          // marker offset of each instance in concatenated arrays
+    co_solver_state *st_all;          // device, n states
+    co_solver_state *st_host;         // pinned
+    co_bwork *d_tab;
+    std::vector<co_bwork> tab;
+    unsigned *d_counter;
+    int total, max_pos;
+    int W, KC, grid, tuned;
+    double tune_ms;
+    int nsm;
+};
+
+__global__ void k_finish_once(int n2, co_solver_state *st, int exit_picard, double *__restrict__ v1,
+                              const double *__restrict__ Gv, const double *__restrict__ vbest) {
+    if (!st->done || st->finished) return;
+    int done = st->done, improved = st->improved;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
+        if (done == 1) {
+            if (exit_picard) v1[i] = Gv[i];
+        } else if (done == 2) {
+            v1[i] = improved ? (exit_picard ? Gv[i] : v1[i]) : vbest[i];
+        } else if (done == 3) {
+            v1[i] = vbest[i];
+        }
+    }
+}
+
+__global__ void k_mark_finished(co_solver_state *st) {
+    if (threadIdx.x == 0 && st->done) st->finished = 1;
+}
+
+static int batch_rebuild_table(co_batch *B) {
+    std::vector<const co_solver_state *> sts(B->n);
+    for (int i = 0; i < B->n; i++) sts[i] = B->st_all + i;
+    B->tab.resize(B->n + 1);
+    int mp = 0;
+    int total = co_batch_work_table(B->ctx.data(), sts.data(), B->n, B->W, B->KC, B->tab.data(), &mp);
+    if (total < 0) return -total;
+    B->tab[B->n] = B->tab[B->n - 1];
+    B->tab[B->n].blk0 = total;  // sentinel
+    B->total = total;
+    B->max_pos = mp;
+    CO_CK(cudaMemcpy(B->d_tab, B->tab.data(), sizeof(co_bwork) * (B->n + 1),
+                     cudaMemcpyHostToDevice));
+    return CO_OK;
+}
+
+extern "C" int co_batch_create(const co_batch_instance *inst, int n, int n_quad, unsigned flags,
+                               int device, co_batch **out) {
+    if (!out || !inst || n < 1) return CO_ERR_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return CO_ERR_NODEVICE;
+    if (device < 0 || device >= ndev) return CO_ERR_ARG;
+    CO_CK(cudaSetDevice(device));
+    co_batch *B = new co_batch();
+    B->device = device;
+    B->n = n;
+    B->W = 4;
+    B->KC = 8;
+    B->tuned = 0;
+    B->tune_ms = 0;
+    cudaDeviceProp prop;
+    cudaGetDeviceProperties(&prop, device);
+    B->nsm = prop.multiProcessorCount;
+    B->grid = 4 * B->nsm;
+    int rc = CO_OK;
+    if (cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete B;
+        return CO_ERR_CUDA;
+    }
+    if (cudaMalloc(&B->st_all, sizeof(co_solver_state) * n) != cudaSuccess ||
+        cudaMallocHost(&B->st_host, sizeof(co_solver_state) * n) != cudaSuccess ||
+        cudaMalloc(&B->d_tab, sizeof(co_bwork) * (n + 1)) != cudaSuccess ||
+        cudaMalloc(&B->d_counter, 64) != cudaSuccess) {
+        co_batch_destroy(B);
+        return CO_ERR_NOMEM;
+    }
+    cudaMemset(B->st_all, 0, sizeof(co_solver_state) * n);
+    size_t off = 0;
+    for (int i = 0; i < n; i++) {
+        const co_batch_instance &d = inst[i];
+        if (d.N < 0 || (d.model != CO_MODEL_LANDAU && d.model != CO_MODEL_LB)) {
+            co_batch_destroy(B);
+            return CO_ERR_ARG;
+        }
+        co_ctx *c = nullptr;
+        rc = co_ctx_create(d.bp1, d.nb1, d.bp2, d.nb2, 2, n_quad, flags, device, &c);
+        if (rc) {
+            co_batch_destroy(B);
+            return rc;
+        }
+        // join the batch: shared stream and state array
+        cudaStreamDestroy(c->stream);
+        c->stream = B->stream;
+        cudaFree(c->st);
+        c->st = B->st_all + i;
+        c->lb_two_pass = 1;
+        c->batch_N = d.N;
+        c->batch_landau = d.model == CO_MODEL_LANDAU;
+        B->ctx.push_back(c);
+        B->N.push_back(d.N);
+        B->model.push_back(d.model);
+        B->nu.push_back(d.nu);
+        B->off.push_back(off);
+        off += (size_t)d.N;
+        if ((rc = co_ensure_capacity(c, d.N, CO_MAX_M))) {
+            co_batch_destroy(B);
+            return rc;
+        }
+    }
+    if ((rc = batch_rebuild_table(B))) {
+        co_batch_destroy(B);
+        return rc;
+    }
+    *out = B;
+    return CO_OK;
+}
+
+extern "C" int co_batch_destroy(co_batch *B) {
+    if (!B) return CO_ERR_ARG;
+    cudaSetDevice(B->device);
+    if (B->stream) cudaStreamSynchronize(B->stream);
+    for (co_ctx *c : B->ctx) {
+        c->st = nullptr;           // owned by the batch
+        c->stream = nullptr;       // shared
+        co_ctx_destroy_detached(c);
+    }
+    if (B->st_all) cudaFree(B->st_all);
+    if (B->st_host) cudaFreeHost(B->st_host);
+    if (B->d_tab) cudaFree(B->d_tab);
+    if (B->d_counter) cudaFree(B->d_counter);
+    if (B->stream) cudaStreamDestroy(B->stream);
+    delete B;
+    return CO_OK;
+}
+
+// everything of one iteration up to the pair sum (Landau) or the whole map (LB)
+static int batch_pre(co_batch *B, int i, const co_opts *o, double S0i, double dt, int *nred) {
+    co_ctx *c = B->ctx[i];
+    co_bufs &b = c->mb;
+    int N = B->N[i], rc;
+    if (N == 0) return CO_OK;
+    if (B->model[i] == CO_MODEL_LB)
+        return picard_map_impl(c, CO_MODEL_LB, o->use_gonzalez, B->nu[i], CO_PREC_FP64, b.Gv, b.v1,
+                               b.v0, N, S0i, dt, b.r, nred);
+    *nred = red_blocks(c, N);
+    if ((rc = landau_geff_dev(c, o->use_gonzalez, b.v1, b.v0, N, S0i))) return rc;
+    return co_pack_landau(c, N, N, CO_PREC_FP64, o->use_gonzalez);
+}
+
+static int batch_iteration(co_batch *B, const co_opts *o, const double *S0, double dt,
+                           const co_dev_opts &d) {
+    int rc;
+    std::vector<int> nred(B->n, 1);
+    for (int i = 0; i < B->n; i++)
+        if ((rc = batch_pre(B, i, o, S0[i], dt, &nred[i]))) return rc;
+    if ((rc = co_pair64_batch(B->stream, B->d_tab, B->n, B->total, B->W, B->KC, B->grid,
+                              B->d_counter, B->max_pos)))
+        return rc;
+    for (int i = 0; i < B->n; i++) {
+        co_ctx *c = B->ctx[i];
+        co_bufs &b = c->mb;
+        int N = B->N[i];
+        if (N == 0) continue;
+        if (B->model[i] == CO_MODEL_LANDAU)
+            if ((rc = co_unpack_update(c, N, dt, b.Gv, b.v0, b.v1, b.r, b.red))) return rc;
+        int n2 = 2 * N, eg = ew_grid(c, n2);
+        size_t ldF = 2 * (size_t)b.cap;
+        k_ctrl1<<<1, 256, 0, B->stream>>>(b.red, nred[i], c->st, d);
+        k_plain_update<<<eg, 256, 0, B->stream>>>(n2, c->st, o->exit_picard_step, b.v1, b.Gv, b.r,
+                                                  b.rp, b.Gp, b.vbest);
+        int ng = red_blocks(c, n2);
+        k_anderson_cols<<<ng, CO_RED_THREADS, 0, B->stream>>>(n2, c->st, b.r, b.rp, b.Gv, b.Gp,
+                                                              b.dF, b.dG, ldF, b.red);
+        k_anderson_solve<<<1, 256, 0, B->stream>>>(b.red, ng, c->st, d);
+        k_anderson_update<<<eg, 256, 0, B->stream>>>(n2, c->st, b.v1, b.Gv, b.dG, ldF);
+        k_finish_once<<<eg, 256, 0, B->stream>>>(n2, c->st, o->exit_picard_step, b.v1, b.Gv,
+                                                 b.vbest);
+        k_mark_finished<<<1, 32, 0, B->stream>>>(c->st);
+        c->launches += 7;
+    }
+    CO_CK(cudaGetLastError());
+    return CO_OK;
+}
+
+extern "C" int co_batch_tune(co_batch *B, int *W, int *KC, int *grid, double *best_ms) {
+    if (!B) return CO_ERR_ARG;
+    CO_CK(cudaSetDevice(B->device));
+    // candidates: tile width, chunk of tile pairs, persistent blocks per SM
+    const int Ws[] = {4, 8};
+    const int KCs[] = {4, 16};
+    const int mults[] = {2, 8};
+    cudaEvent_t e0, e1;
+    CO_CK(cudaEventCreate(&e0));
+    CO_CK(cudaEventCreate(&e1));
+    double best = 1e30;
+    int bW = B->W, bK = B->KC, bG = B->grid;
+    for (int w : Ws)
+        for (int kc : KCs)
+            for (int m : mults) {
+                B->W = w;
+                B->KC = kc;
+                B->grid = m * B->nsm;
+                int rc = batch_rebuild_table(B);
+                if (rc) return rc;
+                CO_CK(cudaEventRecord(e0, B->stream));
+                rc = co_pair64_batch(B->stream, B->d_tab, B->n, B->total, B->W, B->KC, B->grid,
+                                     B->d_counter, B->max_pos);
+                if (rc) return rc;
+                CO_CK(cudaEventRecord(e1, B->stream));
+                CO_CK(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                CO_CK(cudaEventElapsedTime(&ms, e0, e1));
+                if (ms < best) {
+                    best = ms;
+                    bW = w;
+                    bK = kc;
+                    bG = B->grid;
+                }
+            }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    B->W = bW;
+    B->KC = bK;
+    B->grid = bG;
+    B->tuned = 1;
+    B->tune_ms = best;
+    int rc = batch_rebuild_table(B);
+    if (rc) return rc;
+    if (W) *W = bW;
+    if (KC) *KC = bK;
+    if (grid) *grid = bG;
+    if (best_ms) *best_ms = best;
+    return CO_OK;
+}
+
+// concatenated device arrays: instance i's markers are v_all[2*off_i .. 2*off_i + 2*N_i)
+// (its own N x 2 column-major block) and w_all[off_i .. off_i + N_i)
+extern "C" int co_batch_step_dev(co_batch *B, const co_opts *o, double *v1_all,
+                                 const double *v0_all, const double *w_all, const double *S0,
+                                 double dt, int use_graph, int *iters, double *res) {
+    if (!B || !o || !v1_all || !v0_all || !w_all || !S0) return CO_ERR_ARG;
+    if (o->m < 1 || o->m > CO_MAX_M || o->precision != CO_PREC_FP64) return CO_ERR_ARG;
+    CO_CK(cudaSetDevice(B->device));
+    int rc;
+    for (int i = 0; i < B->n; i++) {
+        co_ctx *c = B->ctx[i];
+        size_t n2 = 2 * (size_t)B->N[i] * sizeof(double);
+        CO_CK(cudaMemcpyAsync(c->mb.v1, v1_all + 2 * B->off[i], n2, cudaMemcpyDeviceToDevice,
+                              B->stream));
+        CO_CK(cudaMemcpyAsync(c->mb.v0, v0_all + 2 * B->off[i], n2, cudaMemcpyDeviceToDevice,
+                              B->stream));
+        CO_CK(cudaMemcpyAsync(c->mb.w, w_all + B->off[i], (size_t)B->N[i] * sizeof(double),
+                              cudaMemcpyDeviceToDevice, B->stream));
+        k_state_reset<<<1, 32, 0, B->stream>>>(c->st);
+    }
+    co_dev_opts d = dev_opts(o, 0.0);
+    if (!B->tuned) {
+        // pack every instance once at the initial guess, then time the candidates
+        std::vector<int> nred(B->n);
+        for (int i = 0; i < B->n; i++)
+            if (B->model[i] == CO_MODEL_LANDAU)
+                if ((rc = batch_pre(B, i, o, S0[i], dt, &nred[i]))) return rc;
+        if ((rc = co_batch_tune(B, nullptr, nullptr, nullptr, nullptr))) return rc;
+    }
+    cudaGraphExec_t exec = nullptr;
+    cudaGraph_t graph = nullptr;
+    if (use_graph) {
+        CO_CK(cudaStreamSynchronize(B->stream));
+        CO_CK(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
+        rc = batch_iteration(B, o, S0, dt, d);
+        cudaError_t ce = cudaStreamEndCapture(B->stream, &graph);
+        if (rc) return rc;
+        if (ce != cudaSuccess) return CO_ERR_CUDA;
+        if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
+            cudaGraphDestroy(graph);
+            return CO_ERR_CUDA;
+        }
+    }
+    int k, all_done = 0;
+    for (k = 1; k <= o->max_iter; k++) {
+        if (use_graph) {
+            if (cudaGraphLaunch(exec, B->stream) != cudaSuccess) {
+                rc = CO_ERR_CUDA;
+                break;
+            }
+        } else if ((rc = batch_iteration(B, o, S0, dt, d))) {
+            break;
+        }
+        if (cudaMemcpyAsync(B->st_host, B->st_all, sizeof(co_solver_state) * B->n,
+                            cudaMemcpyDeviceToHost, B->stream) != cudaSuccess ||
+            cudaStreamSynchronize(B->stream) != cudaSuccess) {
+            rc = CO_ERR_CUDA;
+            break;
+        }
+        all_done = 1;
+        for (int i = 0; i < B->n; i++) {
+            if (B->st_host[i].error) rc = B->st_host[i].error;
+            if (!B->st_host[i].finished && B->N[i] > 0) all_done = 0;
+        }
+        if (rc || all_done) break;
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (rc) return rc;
+    // instances still running hit the iteration cap: best iterate (solver.jl:419-422)
+    for (int i = 0; i < B->n; i++) {
+        co_ctx *c = B->ctx[i];
+        int N = B->N[i];
+        if (N == 0) continue;
+        int n2 = 2 * N, eg = ew_grid(c, n2);
+        k_set_done<<<1, 32, 0, B->stream>>>(c->st, 3);
+        k_finish_once<<<eg, 256, 0, B->stream>>>(n2, c->st, o->exit_picard_step, c->mb.v1,
+                                                 c->mb.Gv, c->mb.vbest);
+        k_mark_finished<<<1, 32, 0, B->stream>>>(c->st);
+        CO_CK(cudaMemcpyAsync(v1_all + 2 * B->off[i], c->mb.v1, 2 * (size_t)N * sizeof(double),
+                              cudaMemcpyDeviceToDevice, B->stream));
+    }
+    CO_CK(cudaMemcpyAsync(B->st_host, B->st_all, sizeof(co_solver_state) * B->n,
+                          cudaMemcpyDeviceToHost, B->stream));
+    CO_CK(cudaStreamSynchronize(B->stream));
+    for (int i = 0; i < B->n; i++) {
+        const co_solver_state &s = B->st_host[i];
+        if (iters) iters[i] = (s.done == 3) ? (k > o->max_iter ? o->max_iter : s.k) : s.k;
+        if (res) res[i] = s.res_out;
+    }
+    return CO_OK;
+}
+
+// batch predictor and entropies (per instance, on the batch stream)
+extern "C" int co_batch_predictor_dev(co_batch *B, const co_opts *o, double *v1_all,
+                                      const double *v_all, const double *w_all, double dt) {
+    if (!B || !o || !v1_all || !v_all || !w_all) return CO_ERR_ARG;
+    CO_CK(cudaSetDevice(B->device));
+    int rc;
+    for (int i = 0; i < B->n; i++) {
+        co_ctx *c = B->ctx[i];
+        int N = B->N[i];
+        if (N == 0) continue;
+        co_opts oi = *o;
+        oi.model = B->model[i];
+        oi.nu = B->nu[i];
+        CO_CK(cudaMemcpyAsync(c->mb.v0, v_all + 2 * B->off[i], 2 * (size_t)N * sizeof(double),
+                              cudaMemcpyDeviceToDevice, B->stream));
+        CO_CK(cudaMemcpyAsync(c->mb.w, w_all + B->off[i], (size_t)N * sizeof(double),
+                              cudaMemcpyDeviceToDevice, B->stream));
+        if ((rc = co_predictor_buffers(c, &oi, CO_PREC_FP64, c->mb.v0, N, dt, c->mb.v1))) return rc;
+        CO_CK(cudaMemcpyAsync(v1_all + 2 * B->off[i], c->mb.v1, 2 * (size_t)N * sizeof(double),
+                              cudaMemcpyDeviceToDevice, B->stream));
+    }
+    CO_CK(cudaStreamSynchronize(B->stream));
+    return CO_OK;
+}
+
+extern "C" int co_batch_entropy_dev(co_batch *B, const double *v_all, const double *w_all,
+                                    double *S) {
+    if (!B || !v_all || !w_all || !S) return CO_ERR_ARG;
+    CO_CK(cudaSetDevice(B->device));
+    int rc;
+    for (int i = 0; i < B->n; i++) {
+        co_ctx *c = B->ctx[i];
+        int N = B->N[i];
+        CO_CK(cudaMemcpyAsync(c->mb.w, w_all + B->off[i], (size_t)N * sizeof(double),
+                              cudaMemcpyDeviceToDevice, B->stream));
+        if ((rc = co_sort_markers(c, v_all + 2 * B->off[i], N))) return rc;
+        if ((rc = co_project_sorted(c, c->f))) return rc;
+        if ((rc = co_entropy_parts_dev(c, c->f))) return rc;
+        if ((rc = co_entropy_finalize_dev(c, c->y))) return rc;
+        CO_CK(cudaMemcpyAsync(S + i, c->y, sizeof(double), cudaMemcpyDeviceToHost, B->stream));
+    }
+    CO_CK(cudaStreamSynchronize(B->stream));
+    return CO_OK;
+}
+
+extern "C" int co_batch_launch_count(const co_batch *B, unsigned long long *l) {
+    if (!B || !l) return CO_ERR_ARG;
+    unsigned long long s = 0;
+    for (co_ctx *c : B->ctx) s += c->launches;
+    *l = s;
+    return CO_OK;
+}
+
+// ================================================================ warm start
+
+__global__ void k_dotv_from(int n2, const double *__restrict__ v1, const double *__restrict__ v0,
+                            double inv_dt, double *__restrict__ dotv) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n2) dotv[i] = (v1[i] - v0[i]) * inv_dt;
+}
+
+__global__ void k_ws_apply(int N, const double *__restrict__ vp, const float *__restrict__ Y,
+                           double dt2, double s0, double s1, double h0, double h1,
+                           double *__restrict__ v1) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= N) return;
+    v1[a] = vp[a] + dt2 * ((double)Y[2 * (size_t)a] * s0 + h0);
+    v1[N + a] = vp[N + a] + dt2 * ((double)Y[2 * (size_t)a + 1] * s1 + h1);
+}
+
+extern "C" int co_warmstart_features_dev(co_ctx *c, const co_opts *o, const double *v,
+                                         const double *w, int N, double dt, double *v_pred,
+                                         float *X) {
+    if (!c || !o || N < 0 || (N > 0 && (!v || !w || !v_pred || !X))) return CO_ERR_ARG;
+    CO_CK(cudaSetDevice(c->device));
+    int rc;
+    if ((rc = co_ensure_capacity(c, N, 1))) return rc;
+    if (N == 0) return CO_OK;
+    co_bufs &b = c->mb;
+    CO_CK(cudaMemcpyAsync(b.v0, v, 2 * (size_t)N * sizeof(double), cudaMemcpyDeviceToDevice,
+                          c->stream));
+    CO_CK(cudaMemcpyAsync(b.w, w, (size_t)N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    if ((rc = co_predictor_buffers(c, o, o->precision, b.v0, N, dt, b.v1))) return rc;
+    if (o->model == CO_MODEL_LB) {
+        // dotv of the LB predictor: (v1 - v)/dt is what Gv holds; use it directly
+        k_dotv_from<<<co_cdiv(2LL * N, 256), 256, 0, c->stream>>>(2 * N, b.v1, b.v0, 1.0 / dt,
+                                                                  b.dotv);
+        c->launches++;
+    }
+    if ((rc = co_features_dev(c, b.v0, N, X))) return rc;
+    CO_CK(cudaMemcpyAsync(v_pred, b.v1, 2 * (size_t)N * sizeof(double), cudaMemcpyDeviceToDevice,
+                          c->stream));
+    CO_CK(cudaStreamSynchronize(c->stream));
+    return CO_OK;
+}
+
+extern "C" int co_warmstart_apply_dev(co_ctx *c, const double *v_pred, const float *Y, int N,
+                                      double dt, const double *scale2, const double *shift2,
+                                      double *v1) {
+    if (!c || N < 0 || (N > 0 && (!v_pred || !Y || !v1 || !scale2 || !shift2))) return CO_ERR_ARG;
+    CO_CK(cudaSetDevice(c->device));
+    if (N == 0) return CO_OK;
+    k_ws_apply<<<co_cdiv(N, 256), 256, 0, c->stream>>>(N, v_pred, Y, dt * dt, scale2[0], scale2[1],
+                                                       shift2[0], shift2[1], v1);
+    c->launches++;
+    CO_CK(cudaGetLastError());
+    CO_CK(cudaStreamSynchronize(c->stream));
+    return CO_OK;
+}
+
+extern "C" int co_picard_residual_dev(co_ctx *c, const co_opts *o, const double *v_in,
+                                      const double *v0, const double *w, int N, double S0,
+                                      double dt, double *res) {
+    if (!c || !o || !res || N < 0 || (N > 0 && (!v_in || !v0 || !w))) return CO_ERR_ARG;
+    CO_CK(cudaSetDevice(c->device));
+    int rc;
+    if ((rc = co_ensure_capacity(c, N, 1))) return rc;
+    *res = 0.0;
+    if (N == 0) return CO_OK;
+    co_bufs &b = c->mb;
+    size_t n2 = 2 * (size_t)N * sizeof(double);
+    CO_CK(cudaMemcpyAsync(b.vin, v_in, n2, cudaMemcpyDeviceToDevice, c->stream));
+    CO_CK(cudaMemcpyAsync(b.v0, v0, n2, cudaMemcpyDeviceToDevice, c->stream));
+    CO_CK(cudaMemcpyAsync(b.w, w, (size_t)N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    int nred = 0;
+    if ((rc = picard_map_impl(c, o->model, o->use_gonzalez, o->nu, o->precision, b.Gv, b.vin, b.v0,
+                              N, S0, dt, b.r, &nred)))
+        return rc;
+    co_dev_opts d = dev_opts(o, 0.0);
+    k_state_reset<<<1, 32, 0, c->stream>>>(c->st);
+    k_ctrl1<<<1, 256, 0, c->stream>>>(b.red, nred, c->st, d);
+    c->launches += 2;
+    CO_CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(co_solver_state), cudaMemcpyDeviceToHost,
+                          c->stream));
+    CO_CK(cudaStreamSynchronize(c->stream));
+    *res = c->st_host->nrm_r;
+    return c->st_host->error ? c->st_host->error : CO_OK;
 }

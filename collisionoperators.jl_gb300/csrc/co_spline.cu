@@ -188,21 +188,42 @@ k_perm(const int *__restrict__ cell, int N, const int *__restrict__ hoff,
     }
 }
 
-// segmented sum per (cell, local basis j1 + 3 j2) in marker order
-__global__ void k_cellsum(const int *__restrict__ cstart, const double *__restrict__ sw,
-                          const double *__restrict__ sphi, int n_el, double *__restrict__ bS) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n_el * 9) return;
-    int c = t / 9, j = t - 9 * c;
-    int j1 = j % 3, j2 = j / 3;
-    int p0 = cstart[c], p1 = cstart[c + 1];
-    double acc = 0.0;
-    for (int p = p0; p < p1; p++) {
+// Segmented sum per (cell, local basis j1 + 3 j2): one warp per cell, lane l
+// takes the cell's markers l, l + 32, ... in sorted (index) order and the nine
+// lane sums are combined by a fixed shuffle tree. Cells are very uneven (the
+// central cell of a Gaussian holds ~45x the mean), so the warp, not one thread,
+// walks the segment. Deterministic run to run.
+__global__ void __launch_bounds__(128)
+k_cellsum(const int *__restrict__ cstart, const double *__restrict__ sw,
+          const double *__restrict__ sphi, int n_el, double *__restrict__ bS) {
+    const int c = blockIdx.x * 4 + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (c >= n_el) return;
+    const int p0 = cstart[c], p1 = cstart[c + 1];
+    double acc[9];
+#pragma unroll
+    for (int j = 0; j < 9; j++) acc[j] = 0.0;
+    for (int p = p0 + lane; p < p1; p += 32) {
         const double *ph = sphi + (size_t)p * 6;
-        double val = ph[j1] * ph[3 + j2];
-        acc += sw[p] * val;
+        const double w = sw[p];
+        const double a0 = ph[0], a1 = ph[1], a2 = ph[2], b0 = ph[3], b1 = ph[4], b2 = ph[5];
+        acc[0] += w * (a0 * b0);
+        acc[1] += w * (a1 * b0);
+        acc[2] += w * (a2 * b0);
+        acc[3] += w * (a0 * b1);
+        acc[4] += w * (a1 * b1);
+        acc[5] += w * (a2 * b1);
+        acc[6] += w * (a0 * b2);
+        acc[7] += w * (a1 * b2);
+        acc[8] += w * (a2 * b2);
     }
-    bS[t] = acc;
+#pragma unroll
+    for (int j = 0; j < 9; j++)
+        for (int o = 16; o > 0; o >>= 1) acc[j] += __shfl_down_sync(0xffffffffu, acc[j], o);
+    if (lane == 0) {
+#pragma unroll
+        for (int j = 0; j < 9; j++) bS[(size_t)c * 9 + j] = acc[j];
+    }
 }
 
 // dof k = (k1, k2) gathers the <= 9 cell-local entries that touch it
@@ -428,6 +449,53 @@ k_loggrad(const double *__restrict__ x, int N, const int *__restrict__ cell,
     }
 }
 
+// Warm-start features per marker (after the predictor at x): v, G (entropy
+// gradient), vdot (predictor velocity), log max(f_s, 1e-30) and the clamped
+// grad f_s / f_s, as FP32 rows of 9.
+__global__ void k_features(const double *__restrict__ x, int N, const int *__restrict__ cell,
+                           const double *__restrict__ xi, const double *__restrict__ fc, int n1,
+                           int nd1, const double *__restrict__ bp1, const double *__restrict__ bp2,
+                           const double *__restrict__ C1, const double *__restrict__ C2,
+                           const double *__restrict__ G, const double *__restrict__ vdot,
+                           float *__restrict__ X) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= N) return;
+    int c = cell[a];
+    double f = 0.0, g1 = 0.0, g2 = 0.0;
+    if (c >= 0) {
+        int i = c % n1, j = c / n1;
+        double ih1 = 1.0 / (bp1[i + 1] - bp1[i]), ih2 = 1.0 / (bp2[j + 1] - bp2[j]);
+        double B1[3], dB1[3], B2[3], dB2[3], p1[3], dp1[3], p2[3], dp2[3];
+        bern2(xi[a], B1, dB1);
+        bern2(xi[N + a], B2, dB2);
+        extract3(C1 + 9 * i, B1, p1);
+        extract3(C1 + 9 * i, dB1, dp1);
+        extract3(C2 + 9 * j, B2, p2);
+        extract3(C2 + 9 * j, dB2, dp2);
+        double d1 = 0.0, d2 = 0.0;
+        for (int b = 0; b < 3; b++)
+            for (int q = 0; q < 3; q++) {
+                double cv = fc[(i + q) + (j + b) * nd1];
+                f += cv * (p1[q] * p2[b]);
+                d1 += cv * (dp1[q] * p2[b]) * ih1;
+                d2 += cv * (p1[q] * dp2[b]) * ih2;
+            }
+        double invf = 1.0 / fmax(fabs(f), CO_FS_FLOOR);
+        g1 = fmin(fmax(d1 * invf, -CO_G_MAX), CO_G_MAX);
+        g2 = fmin(fmax(d2 * invf, -CO_G_MAX), CO_G_MAX);
+    }
+    float *o = X + (size_t)a * 9;
+    o[0] = (float)x[a];
+    o[1] = (float)x[N + a];
+    o[2] = (float)G[a];
+    o[3] = (float)G[N + a];
+    o[4] = (float)vdot[a];
+    o[5] = (float)vdot[N + a];
+    o[6] = (float)log(fmax(f, CO_FS_FLOOR));
+    o[7] = (float)g1;
+    o[8] = (float)g2;
+}
+
 // ---------------------------------------------------------------- host side
 
 int co_mid_dv(co_ctx *c, const double *vin, const double *v0, int N) {
@@ -468,8 +536,9 @@ int co_sort_markers(co_ctx *c, const double *x, int N) {
 
 int co_mass_solve_dev(co_ctx *c, const double *rhs, double *out) {
     int n = c->n_dofs;
-    k_mass1<<<co_cdiv(n, 128), 128, 0, c->stream>>>(c->Minv1, rhs, c->nd1, c->nd2, c->y);
-    k_mass2<<<co_cdiv(n, 128), 128, 0, c->stream>>>(c->Minv2, c->y, c->nd1, c->nd2, out);
+    // one warp per block: the FP64 dot products spread over all SMs
+    k_mass1<<<co_cdiv(n, 32), 32, 0, c->stream>>>(c->Minv1, rhs, c->nd1, c->nd2, c->y);
+    k_mass2<<<co_cdiv(n, 32), 32, 0, c->stream>>>(c->Minv2, c->y, c->nd1, c->nd2, out);
     c->launches += 2;
     CO_CK(cudaGetLastError());
     return CO_OK;
@@ -477,9 +546,8 @@ int co_mass_solve_dev(co_ctx *c, const double *rhs, double *out) {
 
 // after co_sort_markers: b = scatter, f = M^{-1} b
 int co_project_sorted(co_ctx *c, double *f_out) {
-    int t = c->n_el * 9;
-    k_cellsum<<<co_cdiv(t, 128), 128, 0, c->stream>>>(c->mb.cstart, c->mb.sw, c->mb.sphi,
-                                                      c->n_el, c->bS);
+    k_cellsum<<<co_cdiv(c->n_el, 4), 128, 0, c->stream>>>(c->mb.cstart, c->mb.sw, c->mb.sphi,
+                                                          c->n_el, c->bS);
     k_dofgather<<<co_cdiv(c->n_dofs, 128), 128, 0, c->stream>>>(c->bS, c->n1, c->n2, c->nd1,
                                                                 c->nd2, c->b);
     c->launches += 2;
@@ -589,6 +657,7 @@ int co_ensure_capacity(co_ctx *c, int N, int m) {
         if ((rc = grow(&b.pf_x, (size_t)cap))) return rc;
         if ((rc = grow(&b.pf_g, (size_t)cap))) return rc;
         if ((rc = grow(&b.pf_w, (size_t)cap))) return rc;
+        if ((rc = grow(&b.pf_wl, (size_t)cap))) return rc;
         if ((rc = grow(&b.pdot, n2))) return rc;
         if ((rc = grow(&b.pA, 3 * (size_t)cap))) return rc;
         int nchunk = co_cdiv(cap, CO_CHUNK);
@@ -612,5 +681,16 @@ int co_ensure_capacity(co_ctx *c, int N, int m) {
         if ((rc = grow(&b.dG, n2 * m))) return rc;
         b.m_cap = m;
     }
+    return CO_OK;
+}
+
+// features at x (cell/xi of x's last sort, coefficients in c->f)
+int co_features_dev(co_ctx *c, const double *x, int N, float *X) {
+    if (N == 0) return CO_OK;
+    k_features<<<co_cdiv(N, 256), 256, 0, c->stream>>>(x, N, c->mb.cell, c->mb.xi, c->f, c->n1,
+                                                       c->nd1, c->bp1, c->bp2, c->C1, c->C2,
+                                                       c->mb.G, c->mb.dotv, X);
+    c->launches++;
+    CO_CK(cudaGetLastError());
     return CO_OK;
 }

@@ -53,6 +53,10 @@ extern "C" {
 /* precision of the implicit solve */
 #define CO_PREC_FP64 0        /* plain FP64 form                                */
 #define CO_PREC_MIXED 1       /* FP32 pair maps, FP64 exit Picard map           */
+#define CO_PREC_MIXED_DS 2    /* FP32 pair maps, then double-single pair maps
+                                 (FP32 head+tail arithmetic, ~44 bits) for the
+                                 FP64 stage; a single map at this precision is
+                                 a double-single map                            */
 
 typedef struct co_ctx co_ctx;
 
@@ -75,7 +79,7 @@ typedef struct {
     double restart_factor;   /* <= 0 means Inf                                  */
     double damping;
     double reg_factor;
-    int precision;           /* CO_PREC_FP64 or CO_PREC_MIXED                   */
+    int precision;           /* CO_PREC_FP64, CO_PREC_MIXED or CO_PREC_MIXED_DS */
     double mixed_floor;      /* mixed form: absolute residual floor of the FP32
                                 phase; <= 0 selects the default                 */
 } co_opts;
@@ -204,6 +208,72 @@ int co_collision_noalloc(const double *v, const double *w, const double *G,
                          double *dot_v, int N, double lo1, double hi1, double lo2,
                          double hi2, void *stream);
 
+/* ---- batched form: many independent ensembles in one engine ----
+ * (no counterpart in the reference, which runs one ensemble per process) */
+typedef struct co_batch co_batch;
+typedef struct {
+    const double *bp1;   /* breakpoints of this instance's mesh */
+    int nb1;
+    const double *bp2;
+    int nb2;
+    int model;           /* CO_MODEL_LANDAU or CO_MODEL_LB */
+    double nu;           /* LB collision frequency          */
+    int N;               /* markers of this instance        */
+} co_batch_instance;
+int co_batch_create(const co_batch_instance *inst, int n, int n_quad, unsigned flags,
+                    int device, co_batch **out);
+int co_batch_destroy(co_batch *batch);
+/* Autotune the batched pair kernel (tile width, tile-pair chunk, persistent
+ * grid) by timing candidates on the current packed operands; the first
+ * co_batch_step_dev does this by itself. */
+int co_batch_tune(co_batch *batch, int *warps, int *chunk, int *grid, double *best_ms);
+/* One implicit step (step_anderson!, FP64) of every instance. Concatenated
+ * device arrays: instance i occupies v[2*off_i, 2*off_i + 2*N_i) (its own
+ * N_i x 2 column-major block, off_i = sum of the N_j before it) and
+ * w[off_i, off_i + N_i). S0[i], iters[i], res[i] are per instance (host).
+ * use_graph != 0 captures one iteration of all instances as a CUDA graph and
+ * replays it until every instance has exited. */
+int co_batch_step_dev(co_batch *batch, const co_opts *opts, double *v1, const double *v0,
+                      const double *w, const double *S0, double dt, int use_graph,
+                      int *iters, double *res);
+int co_batch_predictor_dev(co_batch *batch, const co_opts *opts, double *v1,
+                           const double *v, const double *w, double dt);
+int co_batch_entropy_dev(co_batch *batch, const double *v, const double *w, double *S);
+int co_batch_launch_count(const co_batch *batch, unsigned long long *launches);
+
+/* ---- learned warm start: a small MLP trained by this library's kernels ----
+ * (the reference planned an NN warm start, Parameters.jl:108-117, but its
+ * warmstart_nn.jl is not in the tree). Network n_in -> 64 -> 64 -> 64 -> n_out
+ * with GELU, BF16 weights, FP32 accumulation; MSE loss; Adam. X, T, Y are
+ * DEVICE row-major float arrays (B x n_in, B x n_out). */
+typedef struct co_mlp co_mlp;
+int co_mlp_create(int n_in, int n_out, unsigned seed, int device, co_mlp **out);
+int co_mlp_destroy(co_mlp *mlp);
+int co_mlp_num_params(const co_mlp *mlp, int *P);
+/* FP32 master parameters (host arrays of P floats); the BF16 copy follows. */
+int co_mlp_set_params(co_mlp *mlp, const float *host);
+int co_mlp_get_params(const co_mlp *mlp, float *host);
+int co_mlp_forward(co_mlp *mlp, const float *X, int B, float *Y, void *stream);
+/* gradient of the loss w.r.t. every parameter (host array of P) and the loss */
+int co_mlp_gradients(co_mlp *mlp, const float *X, const float *T, int B, float *grad,
+                     float *loss);
+int co_mlp_train_step(co_mlp *mlp, const float *X, const float *T, int B, float lr,
+                      float *loss);
+/* Per-marker features of the warm start at the start of a step (device
+ * pointers): runs the explicit predictor, writing v_pred, and fills X (N x 9,
+ * row-major): v1, v2, G1, G2 (entropy gradient), vdot1, vdot2 (predictor
+ * velocity), log max(f_s, 1e-30), and grad f_s / f_s (clamped as LOGGRAD_FN). */
+int co_warmstart_features_dev(co_ctx *ctx, const co_opts *opts, const double *v,
+                              const double *w, int N, double dt, double *v_pred, float *X);
+/* v1 = v_pred + dt^2 (Y * scale + shift) per component (device pointers). */
+int co_warmstart_apply_dev(co_ctx *ctx, const double *v_pred, const float *Y, int N,
+                           double dt, const double *scale2, const double *shift2,
+                           double *v1);
+/* ||G(v_in) - v_in|| of one Picard map at opts->precision (device pointers). */
+int co_picard_residual_dev(co_ctx *ctx, const co_opts *opts, const double *v_in,
+                           const double *v0, const double *w, int N, double S0, double dt,
+                           double *res);
+
 /* Number of kernels this context has launched so far. */
 int co_launch_count(const co_ctx *ctx, unsigned long long *launches);
 
@@ -224,6 +294,10 @@ typedef struct {
     unsigned long long pair32_launches;
     double pair32_pairs;
     unsigned long long maps64, maps32;   /* Picard maps by pair precision       */
+    double pairds_ms;                    /* double-single pair kernels           */
+    unsigned long long pairds_launches;
+    double pairds_pairs;
+    unsigned long long mapsds;
 } co_profile_t;
 /* enable != 0 starts (and zeroes) the counters; 0 stops them. */
 int co_profile(co_ctx *ctx, int enable);

@@ -1,0 +1,100 @@
+"""GPU: the warm-start MLP kernels (BF16 weights, FP32 accumulation) against the
+FP64 NumPy oracle, training, and the learned warm start on a small workload.
+
+Tolerances: forward outputs 1e-4 relative (FP32 accumulation of 64-term sums),
+gradients 2e-3 relative in the 2-norm (FP32 per-sample backward and FP32
+minibatch reduction against FP64)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import gaussian_markers, uniform_bp
+
+pytestmark = pytest.mark.gpu
+
+
+def test_mlp_forward_and_gradients_match_oracle(built_lib, collops_mod):
+    import torch
+    from collops import learned
+    from oracle import mlp as om
+    net = learned.MLP(seed=3)
+    p = net.get_params()
+    rng = np.random.default_rng(1)
+    X = rng.standard_normal((1000, 9)).astype(np.float32)
+    T = rng.standard_normal((1000, 2)).astype(np.float32)
+    Xd, Td = torch.from_numpy(X).cuda(), torch.from_numpy(T).cuda()
+    Y = torch.empty((1000, 2), dtype=torch.float32, device="cuda")
+    net.forward(Xd, Y)
+    y_ref, _ = om.forward(p, X.astype(np.float64))
+    assert np.max(np.abs(Y.cpu().numpy() - y_ref)) <= 1e-4 * max(1.0, np.max(np.abs(y_ref)))
+    g, loss = net.gradients(Xd, Td)
+    loss_ref, g_ref = om.loss_and_grad(p, X, T)
+    assert abs(loss - loss_ref) <= 1e-5 * loss_ref
+    assert np.linalg.norm(g - g_ref) <= 2e-3 * np.linalg.norm(g_ref)
+    net.close()
+
+
+def test_mlp_training_reduces_loss(built_lib, collops_mod):
+    import torch
+    from collops import learned
+    rng = np.random.default_rng(2)
+    X = rng.standard_normal((16384, 9)).astype(np.float32)
+    W = rng.standard_normal((9, 2)).astype(np.float32)
+    T = np.tanh(X @ W).astype(np.float32)
+    ws = learned.WarmStart()
+    hist = ws.fit(X, T, epochs=12, batch=2048, lr=3e-3)
+    ws.mlp.close()
+    assert hist[-1] < 0.2 * hist[0]
+
+
+def test_learned_warm_start_small(built_lib, collops_mod, tmp_path):
+    """Generate solver pairs on a small Landau workload, train, and compare the
+    first residual and the iteration count of the next step with and without
+    the learned proposal. The proposal is used only when its first residual is
+    smaller (the fallback rule), so the chosen start is never worse; the gain
+    itself is recorded, not required (the reference measured none)."""
+    import torch
+    from collops import learned
+    bp = uniform_bp(-6.0, 6.0, 16)
+    v, w = gaussian_markers(2048, 1.0, 0.5, seed=9)
+    p = collops_mod.SimParameters(bp1=bp, bp2=bp, m_anderson=5, damping=0.7, tol=1e-12,
+                                  abs_floor=0.0, max_iter=400)
+    ws = collops_mod.build_workspace(p)
+    o = p.opts()
+    dt = 0.02
+    vd = torch.from_numpy(np.ascontiguousarray(v.T)).cuda()
+    wd = torch.from_numpy(w).cuda()
+    lib = ws.lib
+    import ctypes as C
+
+    def solve(v1, x, S0):
+        it, nrs = C.c_int(), C.c_int()
+        res, r0 = C.c_double(), C.c_double()
+        collops_mod._check(lib.co_step_anderson_dev(ws.h, C.byref(o), v1.data_ptr(), x.data_ptr(),
+                                                    wd.data_ptr(), 2048, S0, dt, C.byref(it),
+                                                    C.byref(res), C.byref(nrs), C.byref(r0)),
+                           "step")
+        return it.value
+    X, T, x = learned.generate_pairs(ws, o, vd, wd, dt, 6, solve)
+    assert X.shape == (6 * 2048, 9) and np.all(np.isfinite(X)) and np.all(np.isfinite(T))
+    wsn = learned.WarmStart()
+    hist = wsn.fit(X, T, epochs=30, batch=1024, lr=2e-3)
+    assert hist[-1] < hist[0]
+    path = tmp_path / "ws.npz"
+    wsn.save(str(path))
+    wsn2 = learned.WarmStart.load(str(path))
+    S0 = learned.entropy_of(ws, x, wd)
+    v1 = torch.empty_like(x)
+    used, rl, rp = wsn2.propose(ws, o, x, wd, S0, dt, v1)
+    assert np.isfinite(rl) and np.isfinite(rp)
+    it_learned = solve(v1.clone(), x, S0)
+    vp = torch.empty_like(x)
+    Xf, vp = learned.features(ws, o, x, wd, dt)
+    it_plain = solve(vp.clone(), x, S0)
+    print(f"learned warm start: used={used} r_learned={rl:.3e} r_predictor={rp:.3e} "
+          f"iterations learned-start={it_learned} predictor-start={it_plain}")
+    assert min(rl, rp) <= rp
+    wsn.mlp.close()
+    wsn2.mlp.close()
+    ws.close()

@@ -153,6 +153,25 @@ def test_symmetric_vs_onesided(setup, collops_mod, fp32):
         assert abs(np.sum(w * s[:, 0])) < 1e-13 * np.max(np.abs(s))
 
 
+def test_picard_map_double_single(setup, collops_mod, oracle_mod):
+    """One Landau Picard map with the double-single pair kernel (FP32 head+tail
+    arithmetic, ~44 bits) against the FP64 oracle: 1e-11 relative on v_out."""
+    om, v, w = setup["om"], setup["v"], setup["w"]
+    p = collops_mod.SimParameters(bp1=setup["bp"], bp2=setup["bp"])
+    ws = collops_mod.build_workspace(p)
+    o = oracle_mod.Opts()
+    dt = 0.05
+    S0 = om.entropy(om.l2_project(v, w))
+    v_in = om.predictor(o, v, w, dt)
+    out = np.zeros_like(v, order="F")
+    collops_mod.picard_map(ws, out, v_in, v, w, S0, dt, precision="mixed_ds")
+    ws.close()
+    ref = om.picard_map(o, v_in, v, w, S0, dt)
+    assert np.max(np.abs(out - ref)) / np.max(np.abs(ref)) < 1e-11
+    # the vdot error itself, relative to max |vdot|
+    assert np.max(np.abs(out - ref)) / (dt * np.max(np.abs(ref - v))) < 1e-9
+
+
 def test_collision_mixed(setup, collops_mod, oracle_mod):
     om, v, w = setup["om"], setup["v"], setup["w"]
     p = collops_mod.SimParameters(bp1=setup["bp"], bp2=setup["bp"], gpu_fp32=True)
@@ -266,7 +285,13 @@ def test_step_defect_c1(built_lib, oracle_mod, collops_mod):
     assert abs(info[0] - info_ref[0]) <= 2
     assert np.max(np.abs(x - ref)) / np.max(np.abs(ref)) < 1e-10
     E0 = 0.5 * np.sum(w * (v ** 2).sum(1))
-    for xx, inf in ((x32, info32), (xm, infom)):
+    xd = np.array(v1, order="F", copy=True)
+    ws = collops_mod.build_workspace(collops_mod.SimParameters(bp1=bp, bp2=bp))
+    infod = collops_mod.step_defect(ws, xd, v, w, S0, dt, m=8, tol=1e-12, abs_floor=0.0,
+                                    damping=0.7, max_iter=200, metric64=False,
+                                    precision="mixed_ds")
+    ws.close()
+    for xx, inf in ((x32, info32), (xm, infom), (xd, infod)):
         assert inf[0] < 200 and inf[1] < 1e-12 * np.linalg.norm(xx)
         # an FP64 fixed point of the map (exit Picard update included)
         assert np.linalg.norm(om.picard_map(o, xx, v, w, S0, dt) - xx) < 1e-9
