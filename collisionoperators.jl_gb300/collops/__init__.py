@@ -354,6 +354,12 @@ class Workspace:
         _check(self.lib.co_launch_count(self.h, C.byref(n)), "co_launch_count")
         return n.value
 
+    def stream(self) -> int:
+        """cudaStream_t (as an int) on which the context enqueues all its work."""
+        s = C.c_void_p()
+        _check(self.lib.co_ctx_stream(self.h, C.byref(s)), "co_ctx_stream")
+        return s.value or 0
+
 
 def build_workspace(p: SimParameters, device: int = 0) -> Workspace:
     return Workspace(p, device)

@@ -16,6 +16,7 @@ and records (features at the step start, delta of the converged step).
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes as C
 
 import numpy as np
@@ -62,10 +63,11 @@ class MLP:
         _check(self.lib.co_mlp_set_params(self.h, p.ctypes.data_as(C.POINTER(C.c_float))),
                "co_mlp_set_params")
 
-    def forward(self, X, Y) -> None:
-        """X (B, n_in) and Y (B, n_out): float32 CUDA tensors."""
-        _check(self.lib.co_mlp_forward(self.h, X.data_ptr(), X.shape[0], Y.data_ptr(), None),
-               "co_mlp_forward")
+    def forward(self, X, Y, stream: int = 0) -> None:
+        """X (B, n_in) and Y (B, n_out): float32 CUDA tensors; enqueued on `stream`
+        (a cudaStream_t as an int, 0 = the legacy default stream)."""
+        _check(self.lib.co_mlp_forward(self.h, X.data_ptr(), X.shape[0], Y.data_ptr(),
+                                       C.c_void_p(stream or None)), "co_mlp_forward")
 
     def gradients(self, X, T):
         g = np.zeros(self.P, dtype=np.float32)
@@ -103,12 +105,14 @@ class WarmStart:
         self.xs = np.ones(N_IN)
         self.tm = np.zeros(N_OUT)
         self.ts = np.ones(N_OUT)
+        self._xm_dev = self._xs_dev = None   # device copies of xm, xs
 
     def fit(self, X: np.ndarray, T: np.ndarray, epochs: int = 20, batch: int = 8192,
             lr: float = 2e-3, seed: int = 0, device: int = 0):
         """Train on the GPU with the library's kernels; returns the loss history."""
         import torch
         self.xm, self.xs = X.mean(0), X.std(0) + 1e-12
+        self._xm_dev = None
         self.tm, self.ts = T.mean(0), T.std(0) + 1e-30
         Xn = torch.from_numpy(((X - self.xm) / self.xs).astype(np.float32)).cuda(device)
         Tn = torch.from_numpy(((T - self.tm) / self.ts).astype(np.float32)).cuda(device)
@@ -126,13 +130,19 @@ class WarmStart:
             hist.append(tot / max(cnt, 1))
         return hist
 
-    def predict_delta(self, X):
-        """Normalised features -> delta (float32 CUDA tensors)."""
+    def predict_delta(self, X, stream: int = 0):
+        """Normalised features -> delta (float32 CUDA tensors). With `stream` set,
+        the normalisation and the network run on that stream."""
         import torch
-        Xn = ((X - torch.from_numpy(self.xm.astype(np.float32)).to(X.device)) /
-              torch.from_numpy(self.xs.astype(np.float32)).to(X.device)).contiguous()
-        Y = torch.empty((X.shape[0], N_OUT), dtype=torch.float32, device=X.device)
-        self.mlp.forward(Xn, Y)
+        ctx = (torch.cuda.stream(torch.cuda.ExternalStream(stream, device=X.device))
+               if stream else contextlib.nullcontext())
+        with ctx:
+            if self._xm_dev is None or self._xm_dev.device != X.device:
+                self._xm_dev = torch.from_numpy(self.xm.astype(np.float32)).to(X.device)
+                self._xs_dev = torch.from_numpy(self.xs.astype(np.float32)).to(X.device)
+            Xn = ((X - self._xm_dev) / self._xs_dev).contiguous()
+            Y = torch.empty((X.shape[0], N_OUT), dtype=torch.float32, device=X.device)
+            self.mlp.forward(Xn, Y, stream)
         return Y
 
     def propose(self, ws: Workspace, opts: CoOpts, v, w, S0: float, dt: float, v1_out):
@@ -141,7 +151,9 @@ class WarmStart:
         (used_learned, residual_learned, residual_predictor)."""
         import torch
         X, vp = features(ws, opts, v, w, dt)
-        Y = self.predict_delta(X)
+        # features() returns after the context stream has drained; the network and
+        # everything after it stay on that stream, so co_warmstart_apply_dev sees Y
+        Y = self.predict_delta(X, ws.stream())
         N = v.shape[1]
         vl = torch.empty_like(v)
         sc = np.ascontiguousarray(self.ts, dtype=np.float64)
@@ -156,7 +168,8 @@ class WarmStart:
                                              w.data_ptr(), N, S0, dt, C.byref(rp)),
                "co_picard_residual_dev")
         use = rl.value < rp.value
-        v1_out.copy_(vl if use else vp)
+        with torch.cuda.stream(torch.cuda.ExternalStream(ws.stream(), device=v.device)):
+            v1_out.copy_(vl if use else vp)
         return use, rl.value, rp.value
 
     def save(self, path: str) -> None:
@@ -169,6 +182,7 @@ class WarmStart:
         ws = cls(device=device)
         ws.mlp.set_params(z["params"])
         ws.xm, ws.xs, ws.tm, ws.ts = z["xm"], z["xs"], z["tm"], z["ts"]
+        ws._xm_dev = None
         return ws
 
 

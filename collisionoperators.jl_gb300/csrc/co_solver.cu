@@ -19,7 +19,24 @@
 #include "co_internal.cuh"
 #include "co_reduce.cuh"
 
+#include <stdio.h>
+#include <stdlib.h>
+
 #include <vector>
+
+// COLLOPS_VERBOSE=1 prints the solver's progress to stderr, one line per
+// iteration, as the reference's `verbose = true` does (solver.jl:420, :613-627)
+static int co_verbose() {
+    static int v = -1;
+    if (v < 0) {
+        const char *e = getenv("COLLOPS_VERBOSE");
+        v = (e && *e && *e != '0') ? 1 : 0;
+    }
+    return v;
+}
+static const char *prec_name(int p) {
+    return p == CO_PREC_MIXED ? "fp32" : p == CO_PREC_MIXED_DS ? "ds" : "fp64";
+}
 
 #define CO_RED_COMPS 16
 #define CO_BARRIER_SPINS (1 << 22)
@@ -684,6 +701,11 @@ static int anderson_loop(co_ctx *c, const co_opts *o, int precision, int N, doub
                               c->stream));
         CO_CK(cudaStreamSynchronize(c->stream));
         co_prof_collect(c);
+        if (co_verbose())
+            fprintf(stderr, "    anderson[%s] k=%d  |r|=%.6e  |v|=%.6e%s\n", prec_name(precision), k,
+                    c->st_host->nrm_r, c->st_host->nrm_v,
+                    c->st_host->done == 1 ? "  [converged]"
+                    : c->st_host->done == 2 ? "  [stagnated]" : "");
         if (c->st_host->done) break;
     }
     if (k > max_iter) {
@@ -722,29 +744,17 @@ int co_step_anderson_buffers(co_ctx *c, const co_opts *o, int N, double S0, doub
         if ((rc = anderson_loop(c, o, CO_PREC_MIXED, N, S0, dt, d, o->max_iter, &it))) return rc;
         double r0_32 = c->st_host->nrm_r0;
         int nrs32 = c->st_host->n_restart;
-        // phase 2: the FP64 (or double-single) exit Picard map (exit_picard_step)
-        co_bufs &b = c->mb;
-        int nred = 0;
-        int exit_prec = o->precision == CO_PREC_MIXED_DS ? CO_PREC_MIXED_DS : CO_PREC_FP64;
-        if ((rc = picard_map_impl(c, o->model, o->use_gonzalez, o->nu, exit_prec, b.Gv, b.v1,
-                                  b.v0, N, S0, dt, b.r, &nred)))
-            return rc;
-        co_dev_opts d64 = dev_opts(o, 0.0);
-        d64.max_iter = 1;
-        k_state_reset<<<1, 32, 0, c->stream>>>(c->st);
-        k_ctrl1<<<1, 256, 0, c->stream>>>(b.red, nred, c->st, d64);
-        c->launches += 2;
-        CO_CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(co_solver_state), cudaMemcpyDeviceToHost,
-                              c->stream));
-        CO_CK(cudaStreamSynchronize(c->stream));
-        if (c->st_host->error) return c->st_host->error;
-        if (o->exit_picard_step)
-            CO_CK(cudaMemcpyAsync(b.v1, b.Gv, 2 * (size_t)N * sizeof(double),
-                                  cudaMemcpyDeviceToDevice, c->stream));
-        CO_CK(cudaStreamSynchronize(c->stream));
-        if (iters) *iters = it + 1;
-        if (res) *res = c->st_host->nrm_r;
-        if (nrs) *nrs = nrs32;
+        // phase 2: Anderson on the FP64 (or double-single) map from the phase-1
+        // iterate, to the full tolerance; its exit map is the exit_picard_step
+        const int prec2 = o->precision == CO_PREC_MIXED_DS ? CO_PREC_MIXED_DS : CO_PREC_FP64;
+        const int left = o->max_iter - it > 1 ? o->max_iter - it : 1;
+        int it2 = 0;
+        co_dev_opts d2 = dev_opts(o, 0.0);
+        if ((rc = anderson_loop(c, o, prec2, N, S0, dt, d2, left, &it2))) return rc;
+        if (iters) *iters = it + (c->st_host->done == 0 || c->st_host->done == 3 ? left
+                                                                                 : c->st_host->k);
+        if (res) *res = c->st_host->res_out;
+        if (nrs) *nrs = nrs32 + c->st_host->n_restart;
         if (r0) *r0 = r0_32;
         return CO_OK;
     }
@@ -1029,6 +1039,7 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
         if (c->st_host->error) return c->st_host->error;
         if (c->st_host->done) break;
         int next_stage = stage == 1 ? c->st_host->path : 0;
+        const double outer_nrm = c->st_host->nrm_r;
         // ---- inner: Anderson on the frozen-metric map (u = v1 in place)
         k_state_reset<<<1, 32, 0, c->stream>>>(c->st2);
         c->launches++;
@@ -1055,11 +1066,20 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
             if (c->st_host->done) break;
         }
         total_inner += j > dopt->max_inner ? dopt->max_inner : j;
+        if (co_verbose())
+            fprintf(stderr, "    outer k=%d [%s]  |r|=%.6e  inner +%d%s\n", k,
+                    stage == 1 ? "fp32" : ds ? "ds" : "fp64", outer_nrm,
+                    j > dopt->max_inner ? dopt->max_inner : j,
+                    j > dopt->max_inner ? " (cap)" : "");
         // converged inner solve: u <- Phi(u) (solver.jl:501-503)
         k_copy_if_done<<<eg, 256, 0, c->stream>>>(n2, c->st2, 1, b.v1, b.Phi);
         c->launches++;
         stage = next_stage;
     }
+    if (co_verbose())
+        fprintf(stderr, "    outer k=%d  |r|=%.6e  [%s]\n", k > max_outer ? max_outer : k,
+                c->st_host->nrm_r,
+                c->st_host->done == 1 ? "converged" : c->st_host->done == 2 ? "stagnated" : "cap");
     if (k > max_outer) {
         k_set_done<<<1, 32, 0, c->stream>>>(c->st, 3);
         c->launches++;

@@ -254,6 +254,31 @@ def test_step_anderson_c1(built_lib, oracle_mod, collops_mod, model):
     assert abs(E1 - E0) < 1e-12 * E0
 
 
+@pytest.mark.parametrize("precision", ["mixed", "mixed_ds"])
+def test_step_anderson_mixed_c1(built_lib, oracle_mod, collops_mod, precision):
+    """Mixed-precision step_anderson!: FP32 pair maps, then Anderson on the
+    FP64-accurate (FP64 or double-single) map to the same tolerance. The result
+    is a fixed point of the oracle's FP64 map and conserves momentum and energy."""
+    bp = uniform_bp(-6.0, 6.0, 16)
+    v, w = gaussian_markers(2048, 1.0, 0.5, seed=5)
+    om = oracle_mod.OracleMesh(bp, bp, 6)
+    dt = 0.02
+    o = oracle_mod.Opts(model="landau", m=5, tol=1e-12, abs_floor=0.0, damping=0.7,
+                        max_iter=400)
+    S0 = om.entropy(om.l2_project(v, w))
+    v1 = om.predictor(o, v, w, dt)
+    ws = collops_mod.build_workspace(collops_mod.SimParameters(bp1=bp, bp2=bp))
+    x = np.array(v1, order="F", copy=True)
+    info = collops_mod.step_anderson(ws, x, v, w, S0, dt, m=5, tol=1e-12, abs_floor=0.0,
+                                     damping=0.7, max_iter=400, precision=precision)
+    ws.close()
+    assert info[0] < 400 and info[1] < 1e-12 * np.linalg.norm(x)
+    assert np.linalg.norm(om.picard_map(o, x, v, w, S0, dt) - x) < 1e-9
+    E0 = 0.5 * np.sum(w * (v ** 2).sum(1))
+    assert np.max(np.abs((w[:, None] * (x - v)).sum(0))) < 1e-12
+    assert abs(0.5 * np.sum(w * (x ** 2).sum(1)) - E0) < 1e-12 * E0
+
+
 def test_step_defect_c1(built_lib, oracle_mod, collops_mod):
     """step_defect! against the oracle's (same algorithm, FP64 metric): the same
     fixed point. The implicit step can have several fixed points (two solvers
