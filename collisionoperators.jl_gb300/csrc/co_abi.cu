@@ -179,7 +179,7 @@ static void free_ctx(co_ctx *c) {
                     c->mb.sphi, c->mb.px, c->mb.pg, c->mb.pw, c->mb.pf_x, c->mb.pf_g, c->mb.pf_w, c->mb.pf_wl,
                     c->mb.pdot, c->mb.pA, c->mb.part, c->mb.hist, c->mb.hoff, c->mb.count,
                     c->mb.cstart, c->mb.red, c->mb.dF, c->mb.dG, c->mb.Gk, c->mb.Phi,
-                    c->mb.Adef, c->st2};
+                    c->mb.Adef, c->mb.aa, c->mb.pc, c->st2, c->st3};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     co_prof_free(c);

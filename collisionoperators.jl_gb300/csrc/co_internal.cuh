@@ -74,6 +74,13 @@ struct co_bufs {
     int m_cap;
     // defect correction (allocated on first use)
     double *Gk, *Phi, *Adef;
+    // Anderson mixing of the defect correction's outer iterates (allocated on
+    // first use): vk, u, r, rp, Gp (2 cap each) then dF, dG (2 cap x aa_m each)
+    double *aa;
+    int aa_m;
+    // block-Newton preconditioner of the inner iteration (allocated on first
+    // use): Psi, z (2 cap each) and the Hessian of L (3 cap)
+    double *pc;
 };
 
 struct co_ctx {
@@ -96,6 +103,7 @@ struct co_ctx {
     co_bufs mb;
     co_solver_state *st;     // device state
     co_solver_state *st2;    // inner-solve state of the defect correction
+    co_solver_state *st3;    // outer Anderson window of the defect correction
     co_solver_state *st_host;  // pinned mirror
     double *hstage;          // pinned host staging (grows)
     size_t hstage_cap;
@@ -135,6 +143,7 @@ int co_grad_L_dev(co_ctx *c, const double *x, int N, const double *L, double *G,
 int co_loggrad_dev(co_ctx *c, const double *x, int N, const double *f, double *g,
                    const double *w, const double *dv, double *red);
 int co_mid_dv(co_ctx *c, const double *vin, const double *v0, int N);
+int co_hess_L_dev(co_ctx *c, int N, double *H);
 int co_features_dev(co_ctx *c, const double *x, int N, float *X);
 
 // ------------------------------------------------------------- pair stage

@@ -850,6 +850,38 @@ k_frozen_map(int N, const double *__restrict__ Gv, const double *__restrict__ A,
     }
 }
 
+// Block-Newton preconditioner of the inner iteration (co_defect_opts.precond):
+// per marker, R(u) = Phi(u) - u has the local Jacobian -(I + dt A M), with
+// M = H/2 - (lambda/w) I (G_eff = G(v_mid) - lambda dv/w, v_mid = (u + v0)/2, H
+// the Hessian of L at v_mid). z = (I + dt A M)^{-1} r (plain r where
+// |det| < 0.1) and Psi = u + z, the map Anderson then iterates.
+__global__ void k_precond(int N, const double *__restrict__ A, const double *__restrict__ H,
+                          const double *__restrict__ w, const co_solver_state *st, int use_lambda,
+                          double dt, const double *__restrict__ u, const double *__restrict__ r,
+                          double *__restrict__ z, double *__restrict__ Psi) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= N) return;
+    double lam = use_lambda ? st->lambda : 0.0;
+    double iw = 1.0 / w[a];
+    double A11 = A[a], A12 = A[N + a], A22 = A[2 * (size_t)N + a];
+    double M11 = 0.5 * H[a] - lam * iw, M12 = 0.5 * H[N + a];
+    double M22 = 0.5 * H[2 * (size_t)N + a] - lam * iw;
+    double P11 = 1.0 + dt * (A11 * M11 + A12 * M12);
+    double P12 = dt * (A11 * M12 + A12 * M22);
+    double P21 = dt * (A12 * M11 + A22 * M12);
+    double P22 = 1.0 + dt * (A12 * M12 + A22 * M22);
+    double det = P11 * P22 - P12 * P21;
+    double r1 = r[a], r2 = r[N + a], z1 = r1, z2 = r2;
+    if (fabs(det) >= 0.1) {
+        z1 = (P22 * r1 - P12 * r2) / det;
+        z2 = (P11 * r2 - P21 * r1) / det;
+    }
+    z[a] = z1;
+    z[N + a] = z2;
+    Psi[a] = u[a] + z1;
+    Psi[N + a] = u[N + a] + z2;
+}
+
 struct co_defect_dev {
     double tol, abs_floor, eta, stag_rel_tol, fp32_stall;
     int stag_window;
@@ -961,6 +993,48 @@ k_ctrl_inner(const double *__restrict__ red, int nred, co_solver_state *si,
     }
 }
 
+// Anderson mixing of the outer iterates (co_defect_opts.outer_m > 0): the
+// outer step v_k -> u_k = D(v_k) (the inner solution) is a fixed-point map
+// whose fixed points are those of the Picard map; its slow modes (the part of
+// the Jacobian the frozen metric misses) are removed by mixing over the last
+// outer_m pairs (v_j, u_j). Window control: restart on the first call, when the
+// host flags a change of the pair precision, and when the current outer
+// residual is above twice the best since the last restart; otherwise the next
+// window slot. Undamped (damp = 1): path 0 takes u_k itself.
+__global__ void k_ctrl_aa(co_solver_state *sa, const co_solver_state *so, int m, int restart) {
+    if (threadIdx.x != 0 || so->done) return;
+    const double nr = so->nrm_r;
+    int k = sa->k + 1;
+    sa->improved = 0;
+    sa->damp = 1.0;
+    if (k == 1 || restart || nr > 2.0 * sa->nrm_best) {
+        if (k > 1) sa->n_restart += 1;
+        sa->k = 1;
+        sa->history = 0;
+        sa->slot = 0;
+        sa->path = 0;
+        sa->nrm_best = nr;
+        return;
+    }
+    sa->k = k;
+    if (nr < sa->nrm_best) sa->nrm_best = nr;
+    sa->path = 1;
+    sa->slot = sa->slot % m + 1;
+    sa->history = sa->history + 1 < m ? sa->history + 1 : m;
+}
+
+// u <- D(v_k) (in v1), r <- u - v_k
+__global__ void k_aa_resid(int n2, const co_solver_state *so, const double *__restrict__ v1,
+                           const double *__restrict__ vk, double *__restrict__ u,
+                           double *__restrict__ r) {
+    if (so->done) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
+        double x = v1[i];
+        u[i] = x;
+        r[i] = x - vk[i];
+    }
+}
+
 __global__ void k_copy_if_done(int n2, const co_solver_state *st, int want, double *__restrict__ dst,
                                const double *__restrict__ src) {
     if (st->done != want) return;
@@ -986,6 +1060,31 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
     if (!b.Gk && cudaMalloc(&b.Gk, 2 * sizeof(double) * b.cap) != cudaSuccess) return CO_ERR_NOMEM;
     if (!b.Phi && cudaMalloc(&b.Phi, 2 * sizeof(double) * b.cap) != cudaSuccess) return CO_ERR_NOMEM;
     if (!b.Adef && cudaMalloc(&b.Adef, 3 * sizeof(double) * b.cap) != cudaSuccess) return CO_ERR_NOMEM;
+    const int mo = dopt->outer_m;
+    if (mo < 0 || mo > CO_MAX_M) return CO_ERR_ARG;
+    const size_t ld2 = 2 * (size_t)b.cap;
+    if (mo > 0) {
+        if (!c->st3 && cudaMalloc(&c->st3, sizeof(co_solver_state)) != cudaSuccess)
+            return CO_ERR_NOMEM;
+        if (b.aa && b.aa_m < mo) {
+            cudaFree(b.aa);
+            b.aa = nullptr;
+        }
+        if (!b.aa) {
+            if (cudaMalloc(&b.aa, sizeof(double) * ld2 * (5 + 2 * (size_t)mo)) != cudaSuccess)
+                return CO_ERR_NOMEM;
+            b.aa_m = mo;
+        }
+    }
+    const int pcon = dopt->precond;
+    if (pcon < 0 || pcon > 1) return CO_ERR_ARG;
+    if (pcon && !b.pc && cudaMalloc(&b.pc, 7 * sizeof(double) * b.cap) != cudaSuccess)
+        return CO_ERR_NOMEM;
+    double *pc_Psi = b.pc, *pc_z = b.pc ? b.pc + ld2 : nullptr,
+           *pc_H = b.pc ? b.pc + 2 * ld2 : nullptr;
+    double *aa_vk = b.aa, *aa_u = b.aa + ld2, *aa_r = b.aa + 2 * ld2, *aa_rp = b.aa + 3 * ld2,
+           *aa_Gp = b.aa + 4 * ld2, *aa_dF = b.aa + 5 * ld2,
+           *aa_dG = b.aa + (5 + (size_t)b.aa_m) * ld2;
     const int n2 = 2 * N;
     const size_t ldF = 2 * (size_t)b.cap;
     const int eg = ew_grid(c, n2);
@@ -1005,6 +1104,11 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
     int total_inner = 0;
     k_state_reset<<<1, 32, 0, c->stream>>>(c->st);
     c->launches++;
+    if (mo > 0) {
+        k_state_reset<<<1, 32, 0, c->stream>>>(c->st3);
+        c->launches++;
+    }
+    int aa_stage = -1;   // pair precision of the outer map the window was built on
     int k;
     for (k = 1; k <= max_outer; k++) {
         // ---- outer: G_eff(v_k), F (+ A), G(v_k), residual
@@ -1040,6 +1144,9 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
         if (c->st_host->done) break;
         int next_stage = stage == 1 ? c->st_host->path : 0;
         const double outer_nrm = c->st_host->nrm_r;
+        if (mo > 0)
+            CO_CK(cudaMemcpyAsync(aa_vk, b.v1, n2 * sizeof(double), cudaMemcpyDeviceToDevice,
+                                  c->stream));
         // ---- inner: Anderson on the frozen-metric map (u = v1 in place)
         k_state_reset<<<1, 32, 0, c->stream>>>(c->st2);
         c->launches++;
@@ -1049,14 +1156,25 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
             k_frozen_map<<<nred, CO_RED_THREADS, 0, c->stream>>>(N, b.Gv, b.Adef, b.Gk, b.dS, b.dv,
                                                                b.w, c->st, gz, dt, b.v1, b.Phi, b.r,
                                                                b.red);
+            // the map Anderson iterates and its residual: Phi, r -- or, with the
+            // preconditioner, Psi = u + P^{-1} r and P^{-1} r
+            double *mapv = b.Phi, *res = b.r;
+            if (pcon) {
+                if ((rc = co_hess_L_dev(c, N, pc_H))) return rc;
+                k_precond<<<co_cdiv(N, 256), 256, 0, c->stream>>>(N, b.Adef, pc_H, b.w, c->st, gz,
+                                                                  dt, b.v1, b.r, pc_z, pc_Psi);
+                c->launches++;
+                mapv = pc_Psi;
+                res = pc_z;
+            }
             k_ctrl_inner<<<1, 256, 0, c->stream>>>(b.red, nred, c->st2, c->st, o->m, o->damping);
-            k_plain_update<<<eg, 256, 0, c->stream>>>(n2, c->st2, 0, b.v1, b.Phi, b.r, b.rp, b.Gp,
+            k_plain_update<<<eg, 256, 0, c->stream>>>(n2, c->st2, 0, b.v1, mapv, res, b.rp, b.Gp,
                                                       b.vbest);
             int ng = red_blocks(c, n2);
-            k_anderson_cols<<<ng, CO_RED_THREADS, 0, c->stream>>>(n2, c->st2, b.r, b.rp, b.Phi,
+            k_anderson_cols<<<ng, CO_RED_THREADS, 0, c->stream>>>(n2, c->st2, res, b.rp, mapv,
                                                                   b.Gp, b.dF, b.dG, ldF, b.red);
             k_anderson_solve<<<1, 256, 0, c->stream>>>(b.red, ng, c->st2, di);
-            k_anderson_update<<<eg, 256, 0, c->stream>>>(n2, c->st2, b.v1, b.Phi, b.dG, ldF);
+            k_anderson_update<<<eg, 256, 0, c->stream>>>(n2, c->st2, b.v1, mapv, b.dG, ldF);
             c->launches += 6;
             CO_CK(cudaGetLastError());
             CO_CK(cudaMemcpyAsync(c->st_host, c->st2, sizeof(co_solver_state),
@@ -1074,6 +1192,22 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
         // converged inner solve: u <- Phi(u) (solver.jl:501-503)
         k_copy_if_done<<<eg, 256, 0, c->stream>>>(n2, c->st2, 1, b.v1, b.Phi);
         c->launches++;
+        if (mo > 0) {
+            // v_{k+1} from the window of outer pairs (v_j, D(v_j))
+            k_ctrl_aa<<<1, 32, 0, c->stream>>>(c->st3, c->st, mo, stage != aa_stage);
+            aa_stage = stage;
+            k_aa_resid<<<eg, 256, 0, c->stream>>>(n2, c->st, b.v1, aa_vk, aa_u, aa_r);
+            k_plain_update<<<eg, 256, 0, c->stream>>>(n2, c->st3, 0, aa_vk, aa_u, aa_r, aa_rp,
+                                                      aa_Gp, b.vbest);
+            int ng = red_blocks(c, n2);
+            k_anderson_cols<<<ng, CO_RED_THREADS, 0, c->stream>>>(n2, c->st3, aa_r, aa_rp, aa_u,
+                                                                  aa_Gp, aa_dF, aa_dG, ld2, b.red);
+            k_anderson_solve<<<1, 256, 0, c->stream>>>(b.red, ng, c->st3, di);
+            k_anderson_update<<<eg, 256, 0, c->stream>>>(n2, c->st3, aa_vk, aa_u, aa_dG, ld2);
+            c->launches += 6;
+            CO_CK(cudaMemcpyAsync(b.v1, aa_vk, n2 * sizeof(double), cudaMemcpyDeviceToDevice,
+                                  c->stream));
+        }
         stage = next_stage;
     }
     if (co_verbose())

@@ -449,6 +449,45 @@ k_loggrad(const double *__restrict__ x, int N, const int *__restrict__ cell,
     }
 }
 
+// Hessian of the spline field L at markers x (cell/xi of x's last sort):
+// H = (d11 L, d12 L, d22 L) with the P2 basis' second derivatives
+// d^2 B / dxi^2 = (2, -4, 2); 0 outside the domain. Used by the block-Newton
+// preconditioner of the defect correction's inner iteration.
+__global__ void k_hess_L(int N, const int *__restrict__ cell, const double *__restrict__ xi,
+                         const double *__restrict__ Lc, int n1, int nd1,
+                         const double *__restrict__ bp1, const double *__restrict__ bp2,
+                         const double *__restrict__ C1, const double *__restrict__ C2,
+                         double *__restrict__ H) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= N) return;
+    int c = cell[a];
+    double h11 = 0.0, h12 = 0.0, h22 = 0.0;
+    if (c >= 0) {
+        int i = c % n1, j = c / n1;
+        double ih1 = 1.0 / (bp1[i + 1] - bp1[i]), ih2 = 1.0 / (bp2[j + 1] - bp2[j]);
+        const double d2B[3] = {2.0, -4.0, 2.0};
+        double B1[3], dB1[3], B2[3], dB2[3], p1[3], dp1[3], q1[3], p2[3], dp2[3], q2[3];
+        bern2(xi[a], B1, dB1);
+        bern2(xi[N + a], B2, dB2);
+        extract3(C1 + 9 * i, B1, p1);
+        extract3(C1 + 9 * i, dB1, dp1);
+        extract3(C1 + 9 * i, d2B, q1);
+        extract3(C2 + 9 * j, B2, p2);
+        extract3(C2 + 9 * j, dB2, dp2);
+        extract3(C2 + 9 * j, d2B, q2);
+        for (int b = 0; b < 3; b++)
+            for (int q = 0; q < 3; q++) {
+                double Lv = Lc[(i + q) + (j + b) * nd1];
+                h11 += Lv * (q1[q] * p2[b]) * (ih1 * ih1);
+                h12 += Lv * (dp1[q] * dp2[b]) * (ih1 * ih2);
+                h22 += Lv * (p1[q] * q2[b]) * (ih2 * ih2);
+            }
+    }
+    H[a] = h11;
+    H[N + a] = h12;
+    H[2 * (size_t)N + a] = h22;
+}
+
 // Warm-start features per marker (after the predictor at x): v, G (entropy
 // gradient), vdot (predictor velocity), log max(f_s, 1e-30) and the clamped
 // grad f_s / f_s, as FP32 rows of 9.
@@ -665,11 +704,12 @@ int co_ensure_capacity(co_ctx *c, int N, int m) {
         if ((rc = grow(&b.hoff, (size_t)nchunk * c->n_el))) return rc;
         b.nchunk_cap = nchunk;
         b.cap = cap;
-        double **lazy[] = {&b.Gk, &b.Phi, &b.Adef};  // re-created at the new size on use
+        double **lazy[] = {&b.Gk, &b.Phi, &b.Adef, &b.aa, &b.pc};  // re-created at the new size on use
         for (double **q : lazy) {
             if (*q) cudaFree(*q);
             *q = nullptr;
         }
+        b.aa_m = 0;
         if (b.m_cap > 0) {
             if ((rc = grow(&b.dF, n2 * b.m_cap))) return rc;
             if ((rc = grow(&b.dG, n2 * b.m_cap))) return rc;
@@ -681,6 +721,16 @@ int co_ensure_capacity(co_ctx *c, int N, int m) {
         if ((rc = grow(&b.dG, n2 * m))) return rc;
         b.m_cap = m;
     }
+    return CO_OK;
+}
+
+// Hessian of c->L at x (cell/xi of x's last sort) -> H (3N)
+int co_hess_L_dev(co_ctx *c, int N, double *H) {
+    if (N == 0) return CO_OK;
+    k_hess_L<<<co_cdiv(N, 256), 256, 0, c->stream>>>(N, c->mb.cell, c->mb.xi, c->L, c->n1, c->nd1,
+                                                     c->bp1, c->bp2, c->C1, c->C2, H);
+    c->launches++;
+    CO_CK(cudaGetLastError());
     return CO_OK;
 }
 

@@ -166,6 +166,18 @@ typedef struct {
                        (COLLMETRIC_FN, the reference's path); 0: F from the
                        Newton's-third-law kernel and A from an FP32 kernel (A
                        only shapes the inner model, not the fixed point)      */
+    int outer_m;    /* 0: the reference's outer iteration v_{k+1} = D(v_k), D the
+                       inner solution; 1..8: Anderson mixing of depth outer_m
+                       over the outer iterates (D's fixed points are G's, and
+                       the stopping rule stays on ||G(v) - v||). The window
+                       restarts when the precision stage changes and when the
+                       outer residual exceeds twice its best.                  */
+    int precond;    /* 0: the reference's inner iteration (Anderson on the frozen
+                       map); 1: Anderson on u + P^{-1} (Phi(u) - u) with the
+                       per-marker 2x2 block P = I + dt A (H/2 - (lambda/w) I),
+                       H the Hessian of L at v_mid -- a Newton step for each
+                       marker's locally stiff part. The inner stopping test and
+                       the fixed points are unchanged.                        */
 } co_defect_opts;
 
 /* step_defect! (solver.jl:569-634): defect correction around a frozen

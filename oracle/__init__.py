@@ -55,6 +55,7 @@ def _load():
     lib.om_entropy.argtypes = [C.c_void_p, _dp]
     lib.om_entropy.restype = C.c_double
     lib.om_compute_G.argtypes = [C.c_void_p, _dp, C.c_int, _dp, _dp]
+    lib.om_hessian_L.argtypes = [C.c_void_p, _dp, C.c_int, _dp, _dp]
     lib.om_loggrad.argtypes = [C.c_void_p, _dp, C.c_int, _dp, _dp]
     lib.om_eval_field.argtypes = [C.c_void_p, _dp, C.c_double, C.c_double]
     lib.om_eval_field.restype = C.c_double
@@ -70,7 +71,8 @@ def _load():
                                   C.c_double, C.c_double]
     lib.om_step_anderson.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp, _dp, C.c_int,
                                      C.c_double, C.c_double, _dp]
-    lib.om_step_defect.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_int, _dp,
+    lib.om_step_defect.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int,
+                                   C.c_int, _dp,
                                    _dp, _dp, C.c_int, C.c_double, C.c_double, _dp]
     lib.om_predictor.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp, _dp, C.c_int, C.c_double]
     _lib = lib
@@ -200,6 +202,13 @@ class OracleMesh:
         self.lib.om_compute_G(self.h, _d(v), v.shape[0], _d(L), _d(out))
         return out
 
+    def hessian_L(self, v, L) -> np.ndarray:
+        """(H11, H12, H22) of the spline field L at markers v, shape (N, 3)."""
+        v, L = _mk(v), np.ascontiguousarray(L, dtype=np.float64)
+        out = np.zeros((v.shape[0], 3), order="F")
+        self.lib.om_hessian_L(self.h, _d(v), v.shape[0], _d(L), _d(out))
+        return out
+
     def loggrad(self, v, f) -> np.ndarray:
         v, f = _mk(v), np.ascontiguousarray(f, dtype=np.float64)
         out = np.zeros((v.shape[0], 2), order="F")
@@ -257,14 +266,18 @@ class OracleMesh:
         return v1, (int(out4[0]), out4[1], int(out4[2]), out4[3])
 
     def step_defect(self, opts: Opts, v1, v0, w, S0: float, dt: float, eta: float = 0.05,
-                    max_inner: int = 60, stag_window: int = 5):
-        """step_defect! (solver.jl:569-634) -> (v, (outer, residual, inner, r0))."""
+                    max_inner: int = 60, stag_window: int = 5, outer_m: int = 0,
+                    precond: int = 0):
+        """step_defect! (solver.jl:569-634) -> (v, (outer, residual, inner, r0));
+        outer_m > 0 adds Anderson mixing of the outer iterates, precond = 1 the
+        block-Newton preconditioner of the inner iteration."""
         v1 = np.array(v1, dtype=np.float64, order="F", copy=True)
         v0 = _mk(v0)
         w = np.ascontiguousarray(w, dtype=np.float64)
         out4 = np.zeros(4)
         o = opts.c()
-        self.lib.om_step_defect(self.h, C.byref(o), eta, max_inner, stag_window, _d(v1), _d(v0),
+        self.lib.om_step_defect(self.h, C.byref(o), eta, max_inner, stag_window, outer_m,
+                                int(precond), _d(v1), _d(v0),
                                 _d(w), v0.shape[0], S0, dt, _d(out4))
         return v1, (int(out4[0]), out4[1], int(out4[2]), out4[3])
 

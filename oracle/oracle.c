@@ -837,9 +837,54 @@ void om_predictor(const om_mesh *m, const om_opts *o, double *v1,
 
 /* ---------------------------------------------------------- defect correction */
 
-/* landau_geff! (solver.jl:86-113) at v_in: G_eff and (optionally) v_mid */
+/* Hessian of the spline field L at markers v: (d11, d12, d22) L with the P2
+ * basis' second derivatives d^2 B / dxi^2 = (2, -4, 2); 0 outside the domain.
+ * H is 3N: H11, H12, H22. */
+static void hessian_L(const om_mesh *m, const double *v, int N, const double *Lv, double *H) {
+    static const double d2B[3] = {2.0, -4.0, 2.0};
+    for (int a = 0; a < N; a++) {
+        H[a] = H[N + a] = H[2 * N + a] = 0.0;
+        loc_t L;
+        if (!locate(m, v[a], v[N + a], &L)) continue;
+        double B1[3], dB1[3], B2[3], dB2[3], p1[3], dp1[3], q1[3], p2[3], dp2[3], q2[3];
+        bern2(L.xi1, B1, dB1);
+        bern2(L.xi2, B2, dB2);
+        extract3(m->C1 + 9 * L.i, B1, p1);
+        extract3(m->C1 + 9 * L.i, dB1, dp1);
+        extract3(m->C1 + 9 * L.i, d2B, q1);
+        extract3(m->C2 + 9 * L.j, B2, p2);
+        extract3(m->C2 + 9 * L.j, dB2, dp2);
+        extract3(m->C2 + 9 * L.j, d2B, q2);
+        double ih1 = 1.0 / L.h1, ih2 = 1.0 / L.h2, h11 = 0.0, h12 = 0.0, h22 = 0.0;
+        for (int j2 = 0; j2 < 3; j2++)
+            for (int j1 = 0; j1 < 3; j1++) {
+                double c = Lv[(L.i + j1) + (L.j + j2) * m->nd1];
+                h11 += c * (q1[j1] * p2[j2]) * (ih1 * ih1);
+                h12 += c * (dp1[j1] * dp2[j2]) * (ih1 * ih2);
+                h22 += c * (p1[j1] * q2[j2]) * (ih2 * ih2);
+            }
+        H[a] = h11;
+        H[N + a] = h12;
+        H[2 * N + a] = h22;
+    }
+}
+
+void om_hessian_L(const om_mesh *m, const double *v, int N, const double *Lv, double *H) {
+    hessian_L(m, v, N, Lv, H);
+}
+
+/* landau_geff! (solver.jl:86-113) at v_in: G_eff and (optionally) v_mid; with
+ * H != NULL also the Hessian of L at v_mid and the Gonzalez lambda */
+static void landau_geff_h(const om_mesh *m, int gonzalez, double *Geff, double *vmid,
+                          const double *v_in, const double *v0, const double *w, int N, double S0,
+                          double *H, double *lam_out);
 static void landau_geff(const om_mesh *m, int gonzalez, double *Geff, double *vmid,
                         const double *v_in, const double *v0, const double *w, int N, double S0) {
+    landau_geff_h(m, gonzalez, Geff, vmid, v_in, v0, w, N, S0, NULL, NULL);
+}
+static void landau_geff_h(const om_mesh *m, int gonzalez, double *Geff, double *vmid,
+                          const double *v_in, const double *v0, const double *w, int N, double S0,
+                          double *H, double *lam_out) {
     int nd = m->n_dofs;
     double *dv = malloc(sizeof(double) * 2 * N), *dS = malloc(sizeof(double) * 2 * N);
     double *Gb = malloc(sizeof(double) * 2 * N);
@@ -850,6 +895,7 @@ static void landau_geff(const om_mesh *m, int gonzalez, double *Geff, double *vm
         dv[i] = v_in[i] - v0[i];
     }
     entropy_gradient(m, dS, vmid, w, N, fbuf, r, L, Gb);
+    if (H) hessian_L(m, vmid, N, L, H);
     double corr = 0.0;
     if (gonzalez) {
         om_l2_project(m, v_in, w, N, fbuf);
@@ -861,6 +907,7 @@ static void landau_geff(const om_mesh *m, int gonzalez, double *Geff, double *vm
         }
         corr = nrm2 > 1e-30 ? (S1 - S0 - dot) / nrm2 : 0.0;
     }
+    if (lam_out) *lam_out = corr;
     for (int a = 0; a < N; a++) {
         double iw = 1.0 / w[a];
         Geff[a] = -(dS[a] + corr * dv[a]) * iw;
@@ -875,12 +922,15 @@ typedef struct {
     const double *v0, *w, *Gv, *A, *Gk;
     double S0, dt;
     double *Geff, *vmid;
+    int precond;       /* block-Newton preconditioning of the inner iteration */
+    double *H, lam;    /* Hessian of L at v_mid and lambda of the last map      */
 } frozen_ctx;
 
 /* frozen_map! (solver.jl:585-595) */
 static void frozen_map(frozen_ctx *f, double *out, const double *u) {
     int N = f->N;
-    landau_geff(f->m, f->gonzalez, f->Geff, f->vmid, u, f->v0, f->w, N, f->S0);
+    landau_geff_h(f->m, f->gonzalez, f->Geff, f->vmid, u, f->v0, f->w, N, f->S0,
+                  f->precond ? f->H : NULL, f->precond ? &f->lam : NULL);
     for (int a = 0; a < N; a++) {
         double d1 = f->Geff[a] - f->Gk[a];
         double d2 = f->Geff[N + a] - f->Gk[N + a];
@@ -889,7 +939,34 @@ static void frozen_map(frozen_ctx *f, double *out, const double *u) {
     }
 }
 
-/* _anderson_inner! (solver.jl:492-526); returns the number of map evaluations */
+/* Block-Newton preconditioner of the inner iteration (the library's
+ * extension; precond = 0 is the reference's iteration). Per marker, the
+ * residual R(u) = Phi(u) - u has the local Jacobian -(I + dt A M) with
+ * M = H/2 - (lambda/w) I (H the Hessian of L at v_mid: G_eff = G(v_mid) -
+ * lambda dv / w, v_mid = (u + v0)/2); r <- (I + dt A M)^{-1} r, the 2x2 solve
+ * skipped where |det| < 0.1. The fixed points are unchanged. */
+static void precondition(const frozen_ctx *f, double *r) {
+    int N = f->N;
+    for (int a = 0; a < N; a++) {
+        double iw = 1.0 / f->w[a];
+        double A11 = f->A[a], A12 = f->A[N + a], A22 = f->A[2 * N + a];
+        double M11 = 0.5 * f->H[a] - f->lam * iw, M12 = 0.5 * f->H[N + a];
+        double M22 = 0.5 * f->H[2 * N + a] - f->lam * iw;
+        double P11 = 1.0 + f->dt * (A11 * M11 + A12 * M12);
+        double P12 = f->dt * (A11 * M12 + A12 * M22);
+        double P21 = f->dt * (A12 * M11 + A22 * M12);
+        double P22 = 1.0 + f->dt * (A12 * M12 + A22 * M22);
+        double det = P11 * P22 - P12 * P21;
+        if (!(fabs(det) >= 0.1)) continue;
+        double r1 = r[a], r2 = r[N + a];
+        r[a] = (P22 * r1 - P12 * r2) / det;
+        r[N + a] = (P11 * r2 - P21 * r1) / det;
+    }
+}
+
+/* _anderson_inner! (solver.jl:492-526); returns the number of map evaluations.
+ * With fc->precond, Anderson runs on u + P^{-1} r; the stopping test stays on
+ * the plain residual r. */
 static int anderson_inner(frozen_ctx *fc, double *u, double tol, int maxit, int mm,
                           double damping, double reg_factor) {
     int n = 2 * fc->N;
@@ -906,6 +983,10 @@ static int anderson_inner(frozen_ctx *fc, double *u, double tol, int maxit, int 
             memcpy(u, Fu, sizeof(double) * n);
             ret = k;
             break;
+        }
+        if (fc->precond) {
+            precondition(fc, r);
+            for (int i = 0; i < n; i++) Fu[i] = u[i] + r[i];
         }
         if (k == 1) {
             for (int i = 0; i < n; i++) u[i] = damping * Fu[i] + (1 - damping) * uold[i];
@@ -943,10 +1024,66 @@ static int anderson_inner(frozen_ctx *fc, double *u, double tol, int maxit, int 
     return ret;
 }
 
+/* Anderson mixing of the outer iterates of step_defect! (outer_m > 0; the
+ * library's extension, outer_m = 0 is the reference's iteration). The outer
+ * step v_k -> u_k = D(v_k) (the inner solution) is mixed over the last outer_m
+ * pairs: with r_j = u_j - v_j, dF_j = r_j - r_{j-1}, dU_j = u_j - u_{j-1},
+ * v_{k+1} = u_k - dU gamma, gamma = (dF'dF + l2 I) \ dF' r_k, l2 as in
+ * _anderson_inner! (solver.jl:514-518). The window restarts on the first outer
+ * step and when the outer residual exceeds twice its best since the restart
+ * (then v_{k+1} = u_k). */
+typedef struct {
+    int m, hist, slot, k;
+    double best;
+    double *vk, *u, *r, *rp, *up, *dF, *dU;
+} outer_aa;
+
+static void outer_aa_step(outer_aa *A, double *v1, int n, double nrm, double reg_factor) {
+    int k = A->k + 1;
+    for (int i = 0; i < n; i++) { A->u[i] = v1[i]; A->r[i] = v1[i] - A->vk[i]; }
+    if (k == 1 || nrm > 2.0 * A->best) {
+        A->k = 1;
+        A->hist = 0;
+        A->slot = 0;
+        A->best = nrm;
+    } else {
+        A->k = k;
+        if (nrm < A->best) A->best = nrm;
+        A->slot = A->slot % A->m + 1;
+        A->hist = A->hist + 1 < A->m ? A->hist + 1 : A->m;
+        double *F = A->dF + (size_t)(A->slot - 1) * n, *U = A->dU + (size_t)(A->slot - 1) * n;
+        for (int i = 0; i < n; i++) { F[i] = A->r[i] - A->rp[i]; U[i] = A->u[i] - A->up[i]; }
+        int h = A->hist;
+        double ATA[64], ATr[8];
+        for (int a = 0; a < h; a++) {
+            for (int b = 0; b < h; b++) {
+                double s = 0.0;
+                for (int i = 0; i < n; i++) s += A->dF[(size_t)a * n + i] * A->dF[(size_t)b * n + i];
+                ATA[a * h + b] = s;
+            }
+            double s = 0.0;
+            for (int i = 0; i < n; i++) s += A->dF[(size_t)a * n + i] * A->r[i];
+            ATr[a] = s;
+        }
+        double dm = 0.0;
+        for (int j = 0; j < h; j++) dm += ATA[j * h + j];
+        double l2 = reg_factor * dm / h + 1e-30;
+        for (int j = 0; j < h; j++) ATA[j * h + j] += l2;
+        lu_solve(h, ATA, ATr);
+        for (int i = 0; i < n; i++) {
+            double s = A->u[i];
+            for (int j = 0; j < h; j++) s -= A->dU[(size_t)j * n + i] * ATr[j];
+            v1[i] = s;
+        }
+    }
+    memcpy(A->rp, A->r, sizeof(double) * n);
+    memcpy(A->up, A->u, sizeof(double) * n);
+}
+
 /* step_defect! (solver.jl:569-634). out4 = outer, residual, inner, initial residual */
 void om_step_defect(const om_mesh *m, const om_opts *o, double eta, int max_inner,
-                    int stag_window, double *v1, const double *v0, const double *w, int N,
-                    double S0, double dt, double *out4) {
+                    int stag_window, int outer_m, int precond, double *v1, const double *v0,
+                    const double *w, int N, double S0, double dt, double *out4) {
     int n = 2 * N;
     double *Geff = malloc(sizeof(double) * n), *vmid = malloc(sizeof(double) * n);
     double *dotv = malloc(sizeof(double) * n), *A = malloc(sizeof(double) * 3 * N);
@@ -955,10 +1092,21 @@ void om_step_defect(const om_mesh *m, const om_opts *o, double eta, int max_inne
     double nrm0 = 0.0, nrm_best = INFINITY, nrm_best_window = INFINITY;
     int inner = 0;
     memcpy(vbest, v1, sizeof(double) * n);
-    frozen_ctx fc = {m, o->use_gonzalez, N, v0, w, Gv, A, Gk, S0, dt, NULL, NULL};
+    frozen_ctx fc = {m, o->use_gonzalez, N, v0, w, Gv, A, Gk, S0, dt, NULL, NULL, precond,
+                     NULL, 0.0};
+    double *Hbuf = precond ? malloc(sizeof(double) * 3 * N) : NULL;
+    fc.H = Hbuf;
     double *fGeff = malloc(sizeof(double) * n), *fvmid = malloc(sizeof(double) * n);
     fc.Geff = fGeff;
     fc.vmid = fvmid;
+    outer_aa aa = {outer_m, 0, 0, 0, INFINITY, NULL, NULL, NULL, NULL, NULL, NULL, NULL};
+    if (outer_m > 0) {
+        aa.vk = malloc(sizeof(double) * n); aa.u = malloc(sizeof(double) * n);
+        aa.r = malloc(sizeof(double) * n); aa.rp = malloc(sizeof(double) * n);
+        aa.up = malloc(sizeof(double) * n);
+        aa.dF = calloc((size_t)n * outer_m, sizeof(double));
+        aa.dU = calloc((size_t)n * outer_m, sizeof(double));
+    }
     for (int k = 1; k <= o->max_iter; k++) {
         landau_geff(m, o->use_gonzalez, Geff, vmid, v1, v0, w, N, S0);
         om_collision_metric(m, vmid, w, Geff, N, dotv, A, o->nthreads);
@@ -986,12 +1134,16 @@ void om_step_defect(const om_mesh *m, const om_opts *o, double eta, int max_inne
             nrm_best_window = nrm_best;
         }
         memcpy(Gk, Geff, sizeof(double) * n);
+        if (outer_m > 0) memcpy(aa.vk, v1, sizeof(double) * n);
         inner += anderson_inner(&fc, v1, fmax(eta * nrm, 0.5 * o->abs_floor), max_inner, o->m,
                                 o->damping, o->reg_factor);
+        if (outer_m > 0) outer_aa_step(&aa, v1, n, nrm, o->reg_factor);
     }
     memcpy(v1, vbest, sizeof(double) * n);
     out4[0] = o->max_iter; out4[1] = nrm_best; out4[2] = inner; out4[3] = nrm0;
 done:
     free(Geff); free(vmid); free(dotv); free(A); free(Gv); free(r); free(Gk); free(vbest);
     free(fGeff); free(fvmid);
+    free(aa.vk); free(aa.u); free(aa.r); free(aa.rp); free(aa.up); free(aa.dF); free(aa.dU);
+    free(Hbuf);
 }

@@ -118,6 +118,16 @@ void om_step_anderson(const om_mesh *m, const om_opts *o, double *v1,
  * v1 = v + dt * vdot(v); f_coeffs = l2 projection of v. */
 void om_predictor(const om_mesh *m, const om_opts *o, double *v1,
                   const double *v, const double *w, int N, double dt);
+/* Hessian (d11, d12, d22) of the spline field with coefficients Lv at markers
+ * v (3N out: H11, H12, H22; 0 outside the domain). */
+void om_hessian_L(const om_mesh *m, const double *v, int N, const double *Lv, double *H);
+/* step_defect! (solver.jl:569-634); outer_m > 0 adds Anderson mixing of the
+ * outer iterates and precond = 1 the block-Newton preconditioner of the inner
+ * iteration (0, 0 = the reference's algorithm). v1: guess in, solution out.
+ * out4 = outer iterations, residual, inner iterations, initial residual. */
+void om_step_defect(const om_mesh *m, const om_opts *o, double eta, int max_inner,
+                    int stag_window, int outer_m, int precond, double *v1, const double *v0,
+                    const double *w, int N, double S0, double dt, double *out4);
 
 #ifdef __cplusplus
 }

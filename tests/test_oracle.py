@@ -235,6 +235,70 @@ def test_oracle_step_conserves(oracle_mod, model):
 
 # ---------------------------------------------------- golden vectors
 
+def test_hessian_matches_gradient_differences(mesh16, oracle_mod):
+    """The Hessian gather of the block preconditioner equals central differences
+    of the gradient gather compute_G on the same field (away from cell edges)."""
+    om, bp = mesh16
+    rng = np.random.default_rng(3)
+    L = rng.standard_normal(om.n_dofs)
+    h = bp[1] - bp[0]
+    # markers well inside cells so that +-eps stays in the same cell
+    cells = rng.integers(1, len(bp) - 2, size=(64, 2))
+    v = np.asfortranarray(bp[cells] + h * rng.uniform(0.2, 0.8, size=(64, 2)))
+    H = om.hessian_L(v, L)
+    eps = 1e-6
+    for k, (c1, c2) in enumerate(((0, 0), (1, 1))):
+        e = np.zeros(2)
+        e[k] = eps
+        dG = (om.compute_G(v + e, L) - om.compute_G(v - e, L)) / (2 * eps)
+        np.testing.assert_allclose(H[:, 0 if k == 0 else 2], dG[:, k], rtol=1e-6, atol=1e-6)
+        np.testing.assert_allclose(H[:, 1], dG[:, 1 - k], rtol=1e-6, atol=1e-6)
+
+
+def test_oracle_defect_precond(oracle_mod):
+    """step_defect! with the block-Newton inner preconditioner converges to a
+    fixed point of the FP64 map that conserves momentum and energy, with no more
+    inner maps than the reference's inner iteration."""
+    bp = uniform_bp(-6.0, 6.0, 16)
+    v, w = gaussian_markers(2048, 1.0, 0.5, seed=5)
+    om = oracle_mod.OracleMesh(bp, bp, 6)
+    dt = 0.02
+    o = oracle_mod.Opts(model="landau", m=8, tol=1e-12, abs_floor=0.0, damping=0.7,
+                        max_iter=200, stag_rel_tol=0.1)
+    S0 = om.entropy(om.l2_project(v, w))
+    v1 = om.predictor(o, v, w, dt)
+    _x0, info0 = om.step_defect(o, v1, v, w, S0, dt)
+    x, info = om.step_defect(o, v1, v, w, S0, dt, outer_m=5, precond=1)
+    assert info[1] < 1e-12 * np.linalg.norm(x)
+    assert info[2] <= info0[2]
+    assert np.linalg.norm(om.picard_map(o, x, v, w, S0, dt) - x) < 1e-10
+    assert np.max(np.abs((w[:, None] * (x - v)).sum(0))) < 1e-14
+    E0 = 0.5 * np.sum(w * (v ** 2).sum(1))
+    assert abs(0.5 * np.sum(w * (x ** 2).sum(1)) - E0) < 1e-13 * E0
+
+
+def test_oracle_defect_outer_anderson(oracle_mod):
+    """step_defect! with Anderson mixing of the outer iterates: fewer outer maps
+    than the reference's plain outer iteration on the same step, and the result
+    is a fixed point of the FP64 map that conserves momentum and energy."""
+    bp = uniform_bp(-6.0, 6.0, 16)
+    v, w = gaussian_markers(2048, 1.0, 0.5, seed=5)
+    om = oracle_mod.OracleMesh(bp, bp, 6)
+    dt = 0.02
+    o = oracle_mod.Opts(model="landau", m=8, tol=1e-12, abs_floor=0.0, damping=0.7,
+                        max_iter=200, stag_rel_tol=0.1)
+    S0 = om.entropy(om.l2_project(v, w))
+    v1 = om.predictor(o, v, w, dt)
+    _x0, info0 = om.step_defect(o, v1, v, w, S0, dt, outer_m=0)
+    x, info = om.step_defect(o, v1, v, w, S0, dt, outer_m=5)
+    assert info0[1] < 1e-12 * np.linalg.norm(_x0) and info[1] < 1e-12 * np.linalg.norm(x)
+    assert info[0] < info0[0]
+    assert np.linalg.norm(om.picard_map(o, x, v, w, S0, dt) - x) < 1e-10
+    assert np.max(np.abs((w[:, None] * (x - v)).sum(0))) < 1e-14
+    E0 = 0.5 * np.sum(w * (v ** 2).sum(1))
+    assert abs(0.5 * np.sum(w * (x ** 2).sum(1)) - E0) < 1e-13 * E0
+
+
 def test_golden_vectors(oracle_mod):
     """The oracle reproduces the committed fixture (tests/golden/make_golden.py)."""
     path = os.path.join(GOLDEN, "c1_small.npz")

@@ -279,6 +279,37 @@ def test_step_anderson_mixed_c1(built_lib, oracle_mod, collops_mod, precision):
     assert abs(0.5 * np.sum(w * (x ** 2).sum(1)) - E0) < 1e-12 * E0
 
 
+@pytest.mark.parametrize("precision,precond", [("fp64", 0), ("fp64", 1), ("mixed_ds", 1)])
+def test_step_defect_outer_anderson_c1(built_lib, oracle_mod, collops_mod, precision, precond):
+    """Defect correction with Anderson mixing of the outer iterates (outer_m = 5),
+    with and without the block-Newton inner preconditioner. FP64 with the FP64
+    metric follows the oracle's same algorithm to the same fixed point; the
+    mixed form converges to an FP64 fixed point."""
+    bp = uniform_bp(-6.0, 6.0, 16)
+    v, w = gaussian_markers(2048, 1.0, 0.5, seed=5)
+    om = oracle_mod.OracleMesh(bp, bp, 6)
+    dt = 0.02
+    o = oracle_mod.Opts(model="landau", m=8, tol=1e-12, abs_floor=0.0, damping=0.7,
+                        max_iter=200, stag_rel_tol=0.1)
+    S0 = om.entropy(om.l2_project(v, w))
+    v1 = om.predictor(o, v, w, dt)
+    ref, info_ref = om.step_defect(o, v1, v, w, S0, dt, outer_m=5, precond=precond)
+    ws = collops_mod.build_workspace(collops_mod.SimParameters(bp1=bp, bp2=bp))
+    x = np.array(v1, order="F", copy=True)
+    info = collops_mod.step_defect(ws, x, v, w, S0, dt, m=8, tol=1e-12, abs_floor=0.0,
+                                   damping=0.7, max_iter=200, metric64=precision == "fp64",
+                                   precision=precision, outer_m=5, precond=precond)
+    ws.close()
+    assert info[0] < 200 and info[1] < 1e-12 * np.linalg.norm(x)
+    if precision == "fp64":
+        assert abs(info[0] - info_ref[0]) <= 2
+        assert np.max(np.abs(x - ref)) / np.max(np.abs(ref)) < 1e-10
+    assert np.linalg.norm(om.picard_map(o, x, v, w, S0, dt) - x) < 1e-9
+    E0 = 0.5 * np.sum(w * (v ** 2).sum(1))
+    assert np.max(np.abs((w[:, None] * (x - v)).sum(0))) < 1e-12
+    assert abs(0.5 * np.sum(w * (x ** 2).sum(1)) - E0) < 1e-12 * E0
+
+
 def test_step_defect_c1(built_lib, oracle_mod, collops_mod):
     """step_defect! against the oracle's (same algorithm, FP64 metric): the same
     fixed point. The implicit step can have several fixed points (two solvers
