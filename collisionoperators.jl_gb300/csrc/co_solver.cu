@@ -854,14 +854,15 @@ k_frozen_map(int N, const double *__restrict__ Gv, const double *__restrict__ A,
 // per marker, R(u) = Phi(u) - u has the local Jacobian -(I + dt A M), with
 // M = H/2 - (lambda/w) I (G_eff = G(v_mid) - lambda dv/w, v_mid = (u + v0)/2, H
 // the Hessian of L at v_mid). z = (I + dt A M)^{-1} r (plain r where
-// |det| < 0.1) and Psi = u + z, the map Anderson then iterates.
+// |det| < 0.1) and Psi = u + z, the map Anderson then iterates. use_lambda:
+// 1 with the lambda/w term (Gonzalez on, precond = 1), else M = H/2.
 __global__ void k_precond(int N, const double *__restrict__ A, const double *__restrict__ H,
                           const double *__restrict__ w, const co_solver_state *st, int use_lambda,
                           double dt, const double *__restrict__ u, const double *__restrict__ r,
                           double *__restrict__ z, double *__restrict__ Psi) {
     int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= N) return;
-    double lam = use_lambda ? st->lambda : 0.0;
+    double lam = use_lambda == 1 ? st->lambda : 0.0;
     double iw = 1.0 / w[a];
     double A11 = A[a], A12 = A[N + a], A22 = A[2 * (size_t)N + a];
     double M11 = 0.5 * H[a] - lam * iw, M12 = 0.5 * H[N + a];
@@ -1077,7 +1078,7 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
         }
     }
     const int pcon = dopt->precond;
-    if (pcon < 0 || pcon > 1) return CO_ERR_ARG;
+    if (pcon < 0 || pcon > 2) return CO_ERR_ARG;
     if (pcon && !b.pc && cudaMalloc(&b.pc, 7 * sizeof(double) * b.cap) != cudaSuccess)
         return CO_ERR_NOMEM;
     double *pc_Psi = b.pc, *pc_z = b.pc ? b.pc + ld2 : nullptr,
@@ -1161,8 +1162,9 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
             double *mapv = b.Phi, *res = b.r;
             if (pcon) {
                 if ((rc = co_hess_L_dev(c, N, pc_H))) return rc;
-                k_precond<<<co_cdiv(N, 256), 256, 0, c->stream>>>(N, b.Adef, pc_H, b.w, c->st, gz,
-                                                                  dt, b.v1, b.r, pc_z, pc_Psi);
+                k_precond<<<co_cdiv(N, 256), 256, 0, c->stream>>>(N, b.Adef, pc_H, b.w, c->st,
+                                                                  gz && pcon == 1, dt, b.v1, b.r,
+                                                                  pc_z, pc_Psi);
                 c->launches++;
                 mapv = pc_Psi;
                 res = pc_z;

@@ -176,8 +176,9 @@ typedef struct {
                        map); 1: Anderson on u + P^{-1} (Phi(u) - u) with the
                        per-marker 2x2 block P = I + dt A (H/2 - (lambda/w) I),
                        H the Hessian of L at v_mid -- a Newton step for each
-                       marker's locally stiff part. The inner stopping test and
-                       the fixed points are unchanged.                        */
+                       marker's locally stiff part; 2: the same with M = H/2
+                       (no lambda/w term). The inner stopping test and the
+                       fixed points are unchanged.                            */
 } co_defect_opts;
 
 /* step_defect! (solver.jl:569-634): defect correction around a frozen

@@ -944,14 +944,16 @@ static void frozen_map(frozen_ctx *f, double *out, const double *u) {
  * residual R(u) = Phi(u) - u has the local Jacobian -(I + dt A M) with
  * M = H/2 - (lambda/w) I (H the Hessian of L at v_mid: G_eff = G(v_mid) -
  * lambda dv / w, v_mid = (u + v0)/2); r <- (I + dt A M)^{-1} r, the 2x2 solve
- * skipped where |det| < 0.1. The fixed points are unchanged. */
+ * skipped where |det| < 0.1. precond = 2 drops the lambda/w term (M = H/2).
+ * The fixed points are unchanged. */
 static void precondition(const frozen_ctx *f, double *r) {
     int N = f->N;
     for (int a = 0; a < N; a++) {
         double iw = 1.0 / f->w[a];
         double A11 = f->A[a], A12 = f->A[N + a], A22 = f->A[2 * N + a];
-        double M11 = 0.5 * f->H[a] - f->lam * iw, M12 = 0.5 * f->H[N + a];
-        double M22 = 0.5 * f->H[2 * N + a] - f->lam * iw;
+        double lt = f->precond == 1 ? f->lam * iw : 0.0;   /* mode 2: Hessian only */
+        double M11 = 0.5 * f->H[a] - lt, M12 = 0.5 * f->H[N + a];
+        double M22 = 0.5 * f->H[2 * N + a] - lt;
         double P11 = 1.0 + f->dt * (A11 * M11 + A12 * M12);
         double P12 = f->dt * (A11 * M12 + A12 * M22);
         double P21 = f->dt * (A12 * M11 + A22 * M12);
