@@ -255,7 +255,7 @@ def run_gpu(args, cfg):
         return S.value
 
     dopt = co.CoDefectOpts(args.dc_eta, args.dc_max_inner, args.dc_stag_window, 0.5, 0,
-                           args.dc_outer_m, args.dc_precond)
+                           args.dc_outer_m, args.dc_precond, args.dc_metric_freeze)
 
     warm = None
     if args.warmstart == "learned":
@@ -393,11 +393,18 @@ def run_gpu(args, cfg):
         guess = v1.clone()
         info_h = solve(x_ic, S_ic, args.form, args.solver)
         xh = v1.clone()
+        # the FP64 fixed point nearest the headline result: the same solver on
+        # FP64 pair maps, started from the headline result
+        v1.copy_(xh)
+        info_p = solve(x_ic, S_ic, "fp64", args.solver)
+        xp = v1.clone()
+        # the same solver on FP64 pair maps from the headline's own guess (the
+        # implicit step has several roots; this one may land on another)
         v1.copy_(guess)
         info_64 = solve(x_ic, S_ic, "fp64", args.solver)
         x64 = v1.clone()
         x0 = x_ic.cpu().numpy()
-        ah, a64 = xh.cpu().numpy(), x64.cpu().numpy()
+        ah, a64, ap = xh.cpu().numpy(), x64.cpu().numpy(), xp.cpu().numpy()
         wn = w.cpu().numpy()
         E0 = 0.5 * (wn * (x0 ** 2).sum(0)).sum()
 
@@ -405,10 +412,14 @@ def run_gpu(args, cfg):
             return (float(np.abs((wn * (a - x0)).sum(1)).max()),
                     float(abs(0.5 * (wn * (a ** 2).sum(0)).sum() - E0) / E0))
         acc = dict(
-            reference="the same solver and warm start with FP64 pair maps, from the same guess",
+            reference="the FP64 fixed point reached by the same solver on FP64 pair maps "
+                      "started from the headline result",
             headline=dict(iterations=info_h[0], residual=info_h[1], inner=info_h[2]),
-            fp64=dict(iterations=info_64[0], residual=info_64[1], inner=info_64[2]),
-            vel_err_rel_vs_fp64=float(np.abs(ah - a64).max() / np.abs(a64).max()),
+            fp64_polish=dict(iterations=info_p[0], residual=info_p[1], inner=info_p[2]),
+            vel_err_rel_vs_fp64=float(np.abs(ah - ap).max() / np.abs(ap).max()),
+            fp64_same_guess=dict(iterations=info_64[0], residual=info_64[1], inner=info_64[2],
+                                 root_diff_rel=float(np.abs(ah - a64).max() /
+                                                     np.abs(a64).max())),
             fp64_map_residual_headline=fp64_residual(xh, x_ic, S_ic),
             fp64_map_residual_fp64=fp64_residual(x64, x_ic, S_ic),
             tol_times_norm=cfg["tol"] * float(torch.linalg.vector_norm(xh)),
@@ -644,6 +655,8 @@ def main(argv=None):
     ap.add_argument("--dc-precond", type=int, default=0, choices=[0, 1, 2],
                     help="block-Newton preconditioner of the inner iteration")
     ap.add_argument("--no-accuracy", dest="accuracy", action="store_false")
+    ap.add_argument("--dc-metric-freeze", type=float, default=1e-2,
+                    help="stop rebuilding the FP32 frozen metric once ||r|| < this x ||r_1||")
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--mixed-floor", type=float, default=0.0)

@@ -1110,6 +1110,7 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
         c->launches++;
     }
     int aa_stage = -1;   // pair precision of the outer map the window was built on
+    double first_outer = 0.0, prev_outer = 0.0;   // outer residuals (metric_freeze)
     int k;
     for (k = 1; k <= max_outer; k++) {
         // ---- outer: G_eff(v_k), F (+ A), G(v_k), residual
@@ -1131,9 +1132,14 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
         }
         if (rc) return rc;
         if ((rc = co_unpack_update(c, N, dt, b.Gv, b.v0, b.v1, b.r, b.red))) return rc;
-        if (!m64)
+        // the FP32 metric is rebuilt while the previous outer residual is above
+        // metric_freeze x the first (always at k = 1)
+        const bool new_A = m64 || k == 1 || !(dopt->metric_freeze > 0.0) ||
+                           prev_outer >= dopt->metric_freeze * first_outer;
+        if (!m64 && new_A)
             if ((rc = co_metric32(c, N))) return rc;
-        if ((rc = co_unpack_A(c, N, b.Adef))) return rc;
+        if (new_A)
+            if ((rc = co_unpack_A(c, N, b.Adef))) return rc;
         k_ctrl_outer<<<1, 256, 0, c->stream>>>(b.red, nred, c->st, d, stage);
         k_defect_best<<<eg, 256, 0, c->stream>>>(n2, c->st, b.Gv, b.vbest);
         c->launches += 2;
@@ -1145,6 +1151,8 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
         if (c->st_host->done) break;
         int next_stage = stage == 1 ? c->st_host->path : 0;
         const double outer_nrm = c->st_host->nrm_r;
+        if (k == 1) first_outer = outer_nrm;
+        prev_outer = outer_nrm;
         if (mo > 0)
             CO_CK(cudaMemcpyAsync(aa_vk, b.v1, n2 * sizeof(double), cudaMemcpyDeviceToDevice,
                                   c->stream));

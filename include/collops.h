@@ -179,6 +179,11 @@ typedef struct {
                        marker's locally stiff part; 2: the same with M = H/2
                        (no lambda/w term). The inner stopping test and the
                        fixed points are unchanged.                            */
+    double metric_freeze; /* with metric64 = 0: the FP32 metric A is rebuilt at
+                       outer map k only while ||r_{k-1}|| >= metric_freeze *
+                       ||r_1|| (A only shapes the inner model, so near the
+                       fixed point the last A serves); 0 rebuilds it at every
+                       outer map, as the reference does                       */
 } co_defect_opts;
 
 /* step_defect! (solver.jl:569-634): defect correction around a frozen

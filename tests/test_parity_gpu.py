@@ -310,6 +310,32 @@ def test_step_defect_outer_anderson_c1(built_lib, oracle_mod, collops_mod, preci
     assert abs(0.5 * np.sum(w * (x ** 2).sum(1)) - E0) < 1e-12 * E0
 
 
+def test_step_defect_metric_freeze_c1(built_lib, oracle_mod, collops_mod):
+    """Freezing the FP32 frozen metric once the outer residual has fallen 100x
+    changes only the inner model: the mixed-precision step still converges to a
+    fixed point of the oracle's FP64 map and conserves momentum and energy."""
+    bp = uniform_bp(-6.0, 6.0, 16)
+    v, w = gaussian_markers(2048, 1.0, 0.5, seed=5)
+    om = oracle_mod.OracleMesh(bp, bp, 6)
+    dt = 0.02
+    o = oracle_mod.Opts(model="landau", m=8, tol=1e-12, abs_floor=0.0, damping=0.7,
+                        max_iter=200, stag_rel_tol=0.1)
+    S0 = om.entropy(om.l2_project(v, w))
+    v1 = om.predictor(o, v, w, dt)
+    ws = collops_mod.build_workspace(collops_mod.SimParameters(bp1=bp, bp2=bp))
+    for freeze in (0.0, 1e-2):
+        x = np.array(v1, order="F", copy=True)
+        info = collops_mod.step_defect(ws, x, v, w, S0, dt, m=8, tol=1e-12, abs_floor=0.0,
+                                       damping=0.7, max_iter=200, metric64=False,
+                                       precision="mixed_ds", metric_freeze=freeze)
+        assert info[0] < 200 and info[1] < 1e-12 * np.linalg.norm(x)
+        assert np.linalg.norm(om.picard_map(o, x, v, w, S0, dt) - x) < 1e-9
+        E0 = 0.5 * np.sum(w * (v ** 2).sum(1))
+        assert np.max(np.abs((w[:, None] * (x - v)).sum(0))) < 1e-12
+        assert abs(0.5 * np.sum(w * (x ** 2).sum(1)) - E0) < 1e-12 * E0
+    ws.close()
+
+
 def test_step_defect_c1(built_lib, oracle_mod, collops_mod):
     """step_defect! against the oracle's (same algorithm, FP64 metric): the same
     fixed point. The implicit step can have several fixed points (two solvers
