@@ -499,12 +499,12 @@ k_pair32_sym(const float4 *__restrict__ pfx, const float4 *__restrict__ pfg,
 // from the error-free transformations of Dekker (1971) and Knuth (TAOCP vol. 2):
 // two_sum (6 adds), fast_two_sum (3), two_prod via FMA (2). The intrinsics
 // __fadd_rn/__fsub_rn/__fmul_rn/__fmaf_rn keep the compiler from contracting
-// these sequences. 1/|d| is one Newton step from the MUFU seed. Each ordered
-// pair then costs about 130 FP32 instructions against 11.5 FP64 instructions in
-// k_pair64_sym, i.e. about 5x less issue time on a part whose FP32:FP64 rate is
-// 64:1, at ~1e-13 relative accuracy per term; momentum stays exact to the
-// accumulation round-off because each pair's term is computed once and added
-// with both signs. Used for the FP64 stage of the mixed precision form.
+// these sequences. 1/|d| is one Newton step from the MUFU seed. Each unordered
+// pair (both orders) costs about 180 FP32 instructions against 20 FP64
+// instructions in k_pair64_sym, i.e. about 7x less issue time on a part whose
+// FP32:FP64 rate is 64:1, at ~1e-13 relative accuracy per term; momentum stays
+// exact to the accumulation round-off because each pair's term is computed once
+// and added with both signs. Used for the FP64 stage of the mixed precision form.
 struct dsf {
     float h, l;
 };
@@ -531,34 +531,68 @@ __device__ __forceinline__ dsf ds_mul(dsf a, dsf b) {
     e = __fmaf_rn(a.l, b.h, e);
     return ds_fast(p, e);
 }
-__device__ __forceinline__ dsf ds_mulf(dsf a, float b) {
-    float p = __fmul_rn(a.h, b);
-    float e = __fmaf_rn(a.h, b, -p);
-    e = __fmaf_rn(a.l, b, e);
-    return ds_fast(p, e);
+// Unnormalised double-single values: an intermediate that only feeds a
+// product or a sum is kept as an exact pair (h, l) whose l may exceed
+// ulp(h)/2 by a few ulps; the value h + l carries the same ~2^-44 accuracy,
+// and skipping the renormalising fast_two_sum saves 3 instructions each time.
+__device__ __forceinline__ dsf ds_mul_u(dsf a, dsf b) {   // a b, unnormalised
+    float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    return {p, e};
+}
+__device__ __forceinline__ dsf ds_sqr_u(dsf a) {          // a^2, unnormalised
+    float p = __fmul_rn(a.h, a.h);
+    float e = __fmaf_rn(a.h, a.h, -p);
+    e = __fmaf_rn(__fadd_rn(a.h, a.h), a.l, e);
+    return {p, e};
+}
+__device__ __forceinline__ dsf ds_add_u(dsf a, dsf b) {   // a + b, unnormalised
+    dsf s = ds_two_sum(a.h, b.h);
+    return {s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l))};
+}
+__device__ __forceinline__ dsf ds_norm(dsf a) { return ds_fast(a.h, a.l); }
+// acc += x with acc kept unnormalised (renormalised by the caller every 32 terms)
+__device__ __forceinline__ void ds_acc(dsf &acc, dsf x) {
+    dsf s = ds_two_sum(acc.h, x.h);
+    acc.h = s.h;
+    acc.l = __fadd_rn(acc.l, __fadd_rn(x.l, s.l));
 }
 
-// unweighted pair term u = U(d)(G_a - G_g)/|d| in double-single
-__device__ __forceinline__ void pair_u_ds(const float4 &xg, const float4 &Gg, const float4 &xa,
-                                          const float4 &Ga, dsf &u1, dsf &u2) {
-    dsf d1 = ds_sub({xg.x, xg.z}, {xa.x, xa.z});
-    dsf d2 = ds_sub({xg.y, xg.w}, {xa.y, xa.w});
-    dsf r2 = ds_add(ds_mul(d1, d1), ds_mul(d2, d2));
-    bool ok = r2.h >= 1e-24f;
-    dsf x = ok ? r2 : dsf{1.f, 0.f};
-    float y0 = rsqrtf(x.h);
-    dsf q = ds_mulf(ds_mulf(x, y0), y0);                     // x y0^2 = 1 - e
-    float e = __fsub_rn(__fsub_rn(1.0f, q.h), q.l);
-    dsf y = ds_two_sum(y0, __fmul_rn(__fmul_rn(0.5f, y0), e));  // y0 (1 + e/2)
-    dsf g1 = ds_sub({Ga.x, Ga.z}, {Gg.x, Gg.z});
-    dsf g2 = ds_sub({Ga.y, Ga.w}, {Gg.y, Gg.w});
-    dsf dg = ds_add(ds_mul(d1, g1), ds_mul(d2, g2));
-    dsf cc = ds_mul(dg, ds_mul(y, y));
-    dsf t1 = ds_sub(g1, ds_mul(d1, cc));
-    dsf t2 = ds_sub(g2, ds_mul(d2, cc));
+// Pair term of the symmetric sum in double-single: with u = U(d)(G_a - G_g)/|d|
+// = y t, y = 1/|d|, t = g - d (d.g) y^2, it returns t (unnormalised) and the
+// weighted inverse distances wy_a = w_a y and wy_g = w_g y (0 for |d|^2 < 1e-24),
+// so that the target gets wy_a t and the source -wy_g t.
+__device__ __forceinline__ void pair_t_ds(const float4 &xg, const float4 &Gg, const float4 &xa,
+                                          const float4 &Ga, dsf wa, dsf wg, dsf &t1, dsf &t2,
+                                          dsf &wya, dsf &wyg) {
+    dsf d1 = ds_add_u({xg.x, xg.z}, {-xa.x, -xa.z});
+    dsf d2 = ds_add_u({xg.y, xg.w}, {-xa.y, -xa.w});
+    dsf r2 = ds_add_u(ds_sqr_u(d1), ds_sqr_u(d2));
+    const bool ok = r2.h >= 1e-24f;
+    if (!ok) r2 = {1.f, 0.f};
+    // y = 1/sqrt(r2): MUFU seed y0, then one Newton step y0 (1 + e/2),
+    // e = 1 - r2 y0^2 evaluated with the error terms of both products
+    const float y0 = rsqrtf(r2.h);
+    float p = __fmul_rn(r2.h, y0);
+    float pe = __fmaf_rn(r2.h, y0, -p);
+    pe = __fmaf_rn(r2.l, y0, pe);                  // r2 y0 = p + pe
+    float q = __fmul_rn(p, y0);
+    float qe = __fmaf_rn(p, y0, -q);
+    qe = __fmaf_rn(pe, y0, qe);                    // r2 y0^2 = q + qe
+    const float e = __fsub_rn(__fsub_rn(1.0f, q), qe);
+    dsf y = ds_fast(y0, __fmul_rn(__fmul_rn(0.5f, y0), e));
     if (!ok) y = {0.f, 0.f};
-    u1 = ds_mul(t1, y);
-    u2 = ds_mul(t2, y);
+    dsf g1 = ds_add_u({Ga.x, Ga.z}, {-Gg.x, -Gg.z});
+    dsf g2 = ds_add_u({Ga.y, Ga.w}, {-Gg.y, -Gg.w});
+    dsf dg = ds_add_u(ds_mul_u(d1, g1), ds_mul_u(d2, g2));
+    dsf cc = ds_mul_u(dg, ds_sqr_u(y));
+    dsf m1 = ds_mul_u(d1, cc), m2 = ds_mul_u(d2, cc);
+    t1 = ds_add_u(g1, {-m1.h, -m1.l});
+    t2 = ds_add_u(g2, {-m2.h, -m2.l});
+    wya = ds_mul(wa, y);
+    wyg = ds_mul(wg, y);
 }
 
 __global__ void __launch_bounds__(ST)
@@ -586,11 +620,14 @@ k_pair_ds_sym(const float4 *__restrict__ pfx, const float4 *__restrict__ pfg,
         __syncthreads();
         if (k == 0) {
             for (int a = 0; a < ST; a++) {
-                dsf u1, u2;
-                pair_u_ds(xg, Gg, sx[a], sg[a], u1, u2);
-                dsf wa = {sw[a].x, sw[a].y};
-                ga1 = ds_add(ga1, ds_mul(wa, u1));
-                ga2 = ds_add(ga2, ds_mul(wa, u2));
+                dsf t1, t2, wya, wyg;
+                pair_t_ds(xg, Gg, sx[a], sg[a], {sw[a].x, sw[a].y}, wg, t1, t2, wya, wyg);
+                ds_acc(ga1, ds_mul_u(wya, t1));
+                ds_acc(ga2, ds_mul_u(wya, t2));
+                if ((a & 31) == 31) {
+                    ga1 = ds_norm(ga1);
+                    ga2 = ds_norm(ga2);
+                }
             }
         } else {
             for (int r = 0; r < 4; r++) {
@@ -600,19 +637,23 @@ k_pair_ds_sym(const float4 *__restrict__ pfx, const float4 *__restrict__ pfg,
 #pragma unroll 2
                 for (int q = 0; q < 32; q++) {
                     const int ai = base + ((lane + q) & 31);
-                    dsf u1, u2;
-                    pair_u_ds(xg, Gg, sx[ai], sg[ai], u1, u2);
-                    dsf wa = {sw[ai].x, sw[ai].y};
-                    ga1 = ds_add(ga1, ds_mul(wa, u1));
-                    ga2 = ds_add(ga2, ds_mul(wa, u2));
-                    a1 = ds_sub(a1, ds_mul(wg, u1));
-                    a2 = ds_sub(a2, ds_mul(wg, u2));
+                    dsf t1, t2, wya, wyg;
+                    pair_t_ds(xg, Gg, sx[ai], sg[ai], {sw[ai].x, sw[ai].y}, wg, t1, t2, wya, wyg);
+                    ds_acc(ga1, ds_mul_u(wya, t1));
+                    ds_acc(ga2, ds_mul_u(wya, t2));
+                    const dsf nw = {-wyg.h, -wyg.l};
+                    ds_acc(a1, ds_mul_u(nw, t1));
+                    ds_acc(a2, ds_mul_u(nw, t2));
                     const int src = (lane + 1) & 31;
                     a1.h = __shfl_sync(0xffffffffu, a1.h, src);
                     a1.l = __shfl_sync(0xffffffffu, a1.l, src);
                     a2.h = __shfl_sync(0xffffffffu, a2.h, src);
                     a2.l = __shfl_sync(0xffffffffu, a2.l, src);
                 }
+                a1 = ds_norm(a1);
+                a2 = ds_norm(a2);
+                ga1 = ds_norm(ga1);
+                ga2 = ds_norm(ga2);
                 sacc[base + lane] = make_float4(a1.h, a1.l, a2.h, a2.l);
                 __syncthreads();
             }

@@ -6,10 +6,12 @@ gradients 2e-3 relative in the 2-norm (FP32 per-sample backward and FP32
 minibatch reduction against FP64)."""
 from __future__ import annotations
 
+import os
+
 import numpy as np
 import pytest
 
-from conftest import gaussian_markers, uniform_bp
+from conftest import PKG, gaussian_markers, uniform_bp
 
 pytestmark = pytest.mark.gpu
 
@@ -98,3 +100,51 @@ def test_learned_warm_start_small(built_lib, collops_mod, tmp_path):
     wsn.mlp.close()
     wsn2.mlp.close()
     ws.close()
+
+
+def test_trained_warm_start_gain(built_lib, collops_mod):
+    """The committed network (trained by collops.train_warmstart on >= 1M pairs
+    from the N = 131,072 workload and the batched family) on held-out Landau
+    instances of that family: its proposal's first residual is well below the
+    explicit predictor's. The solve from each start is reported beside it; the
+    first-residual gain is what the network buys (a few outer iterations at most,
+    since each defect-correction outer map cuts the residual ~5x)."""
+    import ctypes as C
+
+    import torch
+    from collops import learned
+    path = os.path.join(PKG, "collops", "warmstart_c3.npz")
+    warm = learned.WarmStart.load(path)
+    gains = []
+    for N, n, sx, sy, seed in ((16384, 32, 0.9, 0.6, 501), (32768, 40, 1.1, 0.7, 502)):
+        bp = uniform_bp(-6.0, 6.0, n)
+        v, w = gaussian_markers(N, sx, sy, seed=seed)
+        p = collops_mod.SimParameters(bp1=bp, bp2=bp, m_anderson=8, damping=0.7, tol=1e-12,
+                                      abs_floor=0.0, max_iter=400, precision="mixed_ds")
+        ws = collops_mod.build_workspace(p)
+        o = p.opts()
+        dt = 0.02
+        x = torch.from_numpy(np.ascontiguousarray(v.T)).cuda()
+        wd = torch.from_numpy(w).cuda()
+        S0 = learned.entropy_of(ws, x, wd)
+        v1 = torch.empty_like(x)
+        used, rl, rp = warm.propose(ws, o, x, wd, S0, dt, v1)
+        _X, vp = learned.features(ws, o, x, wd, dt)
+        its = []
+        for start in (v1.clone(), vp.clone()):
+            it, inner = C.c_int(), C.c_int()
+            res, r0 = C.c_double(), C.c_double()
+            d = collops_mod.CoDefectOpts(0.05, 60, 5, 0.5, 0, 0, 0, 1e-2)
+            oo = p.opts()
+            oo.stag_rel_tol = 0.1
+            collops_mod._check(ws.lib.co_step_defect_dev(
+                ws.h, C.byref(oo), C.byref(d), start.data_ptr(), x.data_ptr(), wd.data_ptr(), N,
+                S0, dt, C.byref(it), C.byref(res), C.byref(inner), C.byref(r0)), "defect")
+            its.append((it.value, inner.value, res.value))
+        ws.close()
+        print(f"N={N}: first residual learned {rl:.3e} predictor {rp:.3e} (x{rp / rl:.2f}); "
+              f"outer/inner learned {its[0][:2]} predictor {its[1][:2]}")
+        assert used and rl < 0.8 * rp
+        gains.append(rp / rl)
+    warm.mlp.close()
+    assert min(gains) > 1.25
