@@ -145,8 +145,8 @@ _SIGNATURES = {
     "co_mlp_train_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_float,
                                     C.POINTER(C.c_float)]),
     "co_warmstart_features_dev": (C.c_int, [C.c_void_p, C.POINTER(CoOpts), C.c_void_p,
-                                            C.c_void_p, C.c_int, C.c_double, C.c_void_p,
-                                            C.c_void_p]),
+                                            C.c_void_p, C.c_int, C.c_double, C.c_double,
+                                            C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
     "co_warmstart_apply_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                          C.c_double, _dp, _dp, C.c_void_p]),
     "co_picard_residual_dev": (C.c_int, [C.c_void_p, C.POINTER(CoOpts), C.c_void_p, C.c_void_p,

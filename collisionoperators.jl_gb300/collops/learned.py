@@ -23,7 +23,7 @@ import numpy as np
 
 from . import CollopsError, CoOpts, Workspace, _check, _p, load_library
 
-N_IN, N_OUT = 9, 2
+N_IN, N_OUT = 15, 2   # features per marker (co_warmstart_features_dev), outputs
 
 
 class MLP:
@@ -84,16 +84,18 @@ class MLP:
         return loss.value
 
 
-def features(ws: Workspace, opts: CoOpts, v, w, dt: float):
-    """(X float32 (N, 9), v_pred) on the device for markers v (torch (2, N))."""
+def features(ws: Workspace, opts: CoOpts, v, w, S0: float, dt: float):
+    """(X float32 (N, 15), v_pred, ||G(v_pred) - v_pred||) on the device for
+    markers v (torch (2, N)) whose projection has entropy S0."""
     import torch
     N = v.shape[1]
     X = torch.empty((N, N_IN), dtype=torch.float32, device=v.device)
     vp = torch.empty_like(v)
+    rp = C.c_double()
     _check(ws.lib.co_warmstart_features_dev(ws.h, C.byref(opts), v.data_ptr(), w.data_ptr(), N,
-                                            dt, vp.data_ptr(), X.data_ptr()),
+                                            S0, dt, vp.data_ptr(), X.data_ptr(), C.byref(rp)),
            "co_warmstart_features_dev")
-    return X, vp
+    return X, vp, rp.value
 
 
 class WarmStart:
@@ -150,7 +152,7 @@ class WarmStart:
         residual is smaller than the predictor's, else the predictor. Returns
         (used_learned, residual_learned, residual_predictor)."""
         import torch
-        X, vp = features(ws, opts, v, w, dt)
+        X, vp, rp_pred = features(ws, opts, v, w, S0, dt)
         # features() returns after the context stream has drained; the network and
         # everything after it stay on that stream, so co_warmstart_apply_dev sees Y
         Y = self.predict_delta(X, ws.stream())
@@ -160,17 +162,14 @@ class WarmStart:
         sh = np.ascontiguousarray(self.tm, dtype=np.float64)
         _check(ws.lib.co_warmstart_apply_dev(ws.h, vp.data_ptr(), Y.data_ptr(), N, dt, _p(sc),
                                              _p(sh), vl.data_ptr()), "co_warmstart_apply_dev")
-        rl, rp = C.c_double(), C.c_double()
+        rl = C.c_double()
         _check(ws.lib.co_picard_residual_dev(ws.h, C.byref(opts), vl.data_ptr(), v.data_ptr(),
                                              w.data_ptr(), N, S0, dt, C.byref(rl)),
                "co_picard_residual_dev")
-        _check(ws.lib.co_picard_residual_dev(ws.h, C.byref(opts), vp.data_ptr(), v.data_ptr(),
-                                             w.data_ptr(), N, S0, dt, C.byref(rp)),
-               "co_picard_residual_dev")
-        use = rl.value < rp.value
+        use = rl.value < rp_pred
         with torch.cuda.stream(torch.cuda.ExternalStream(ws.stream(), device=v.device)):
             v1_out.copy_(vl if use else vp)
-        return use, rl.value, rp.value
+        return use, rl.value, rp_pred
 
     def save(self, path: str) -> None:
         np.savez_compressed(path, params=self.mlp.get_params(), xm=self.xm, xs=self.xs,
@@ -195,7 +194,7 @@ def generate_pairs(ws: Workspace, opts: CoOpts, v, w, dt: float, steps: int, sol
     x = v.clone()
     for _ in range(steps):
         S0 = entropy_of(ws, x, w)
-        X, vp = features(ws, opts, x, w, dt)
+        X, vp, _rp = features(ws, opts, x, w, S0, dt)
         v1 = vp.clone()
         solve(v1, x, S0)
         delta = ((v1 - vp) / (dt * dt)).T.contiguous()

@@ -500,7 +500,7 @@ k_pair32_sym(const float4 *__restrict__ pfx, const float4 *__restrict__ pfg,
 // two_sum (6 adds), fast_two_sum (3), two_prod via FMA (2). The intrinsics
 // __fadd_rn/__fsub_rn/__fmul_rn/__fmaf_rn keep the compiler from contracting
 // these sequences. 1/|d| is one Newton step from the MUFU seed. Each unordered
-// pair (both orders) costs about 180 FP32 instructions against 20 FP64
+// pair (both orders) costs about 190 FP32 instructions against 20 FP64
 // instructions in k_pair64_sym, i.e. about 7x less issue time on a part whose
 // FP32:FP64 rate is 64:1, at ~1e-13 relative accuracy per term; momentum stays
 // exact to the accumulation round-off because each pair's term is computed once
@@ -535,6 +535,8 @@ __device__ __forceinline__ dsf ds_mul(dsf a, dsf b) {
 // product or a sum is kept as an exact pair (h, l) whose l may exceed
 // ulp(h)/2 by a few ulps; the value h + l carries the same ~2^-44 accuracy,
 // and skipping the renormalising fast_two_sum saves 3 instructions each time.
+// The products drop the l*l term, so a factor whose l can be large relative to
+// h (a difference of nearly equal inputs) is renormalised first.
 __device__ __forceinline__ dsf ds_mul_u(dsf a, dsf b) {   // a b, unnormalised
     float p = __fmul_rn(a.h, b.h);
     float e = __fmaf_rn(a.h, b.h, -p);
@@ -567,8 +569,10 @@ __device__ __forceinline__ void ds_acc(dsf &acc, dsf x) {
 __device__ __forceinline__ void pair_t_ds(const float4 &xg, const float4 &Gg, const float4 &xa,
                                           const float4 &Ga, dsf wa, dsf wg, dsf &t1, dsf &t2,
                                           dsf &wya, dsf &wyg) {
-    dsf d1 = ds_add_u({xg.x, xg.z}, {-xa.x, -xa.z});
-    dsf d2 = ds_add_u({xg.y, xg.w}, {-xa.y, -xa.w});
+    // differences are renormalised: for close markers the heads cancel exactly
+    // and the tail difference would otherwise be a large l (the products drop l*l)
+    dsf d1 = ds_norm(ds_add_u({xg.x, xg.z}, {-xa.x, -xa.z}));
+    dsf d2 = ds_norm(ds_add_u({xg.y, xg.w}, {-xa.y, -xa.w}));
     dsf r2 = ds_add_u(ds_sqr_u(d1), ds_sqr_u(d2));
     const bool ok = r2.h >= 1e-24f;
     if (!ok) r2 = {1.f, 0.f};
@@ -584,8 +588,8 @@ __device__ __forceinline__ void pair_t_ds(const float4 &xg, const float4 &Gg, co
     const float e = __fsub_rn(__fsub_rn(1.0f, q), qe);
     dsf y = ds_fast(y0, __fmul_rn(__fmul_rn(0.5f, y0), e));
     if (!ok) y = {0.f, 0.f};
-    dsf g1 = ds_add_u({Ga.x, Ga.z}, {-Gg.x, -Gg.z});
-    dsf g2 = ds_add_u({Ga.y, Ga.w}, {-Gg.y, -Gg.w});
+    dsf g1 = ds_norm(ds_add_u({Ga.x, Ga.z}, {-Gg.x, -Gg.z}));
+    dsf g2 = ds_norm(ds_add_u({Ga.y, Ga.w}, {-Gg.y, -Gg.w}));
     dsf dg = ds_add_u(ds_mul_u(d1, g1), ds_mul_u(d2, g2));
     dsf cc = ds_mul_u(dg, ds_sqr_u(y));
     dsf m1 = ds_mul_u(d1, cc), m2 = ds_mul_u(d2, cc);

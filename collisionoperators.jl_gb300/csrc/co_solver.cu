@@ -1271,6 +1271,7 @@ struct co_batch {
     std::vector<co_bwork> tab;
     unsigned *d_counter;
     int total, max_pos;
+    std::vector<int> live;            // instances still iterating (table and graph cover these)
     int W, KC, grid, tuned;
     double tune_ms;
     int nsm;
@@ -1295,19 +1296,30 @@ __global__ void k_mark_finished(co_solver_state *st) {
     if (threadIdx.x == 0 && st->done) st->finished = 1;
 }
 
+// work table of the batched pair kernel over the live instances (B->live)
 static int batch_rebuild_table(co_batch *B) {
-    std::vector<const co_solver_state *> sts(B->n);
-    for (int i = 0; i < B->n; i++) sts[i] = B->st_all + i;
-    B->tab.resize(B->n + 1);
+    const int n = (int)B->live.size();
+    if (n == 0) {
+        B->total = 0;
+        return CO_OK;
+    }
+    std::vector<co_ctx *> cs(n);
+    std::vector<const co_solver_state *> sts(n);
+    for (int j = 0; j < n; j++) {
+        cs[j] = B->ctx[B->live[j]];
+        sts[j] = B->st_all + B->live[j];
+    }
+    B->tab.resize(n + 1);
     int mp = 0;
-    int total = co_batch_work_table(B->ctx.data(), sts.data(), B->n, B->W, B->KC, B->tab.data(), &mp);
+    int total = co_batch_work_table(cs.data(), sts.data(), n, B->W, B->KC, B->tab.data(), &mp);
     if (total < 0) return -total;
-    B->tab[B->n] = B->tab[B->n - 1];
-    B->tab[B->n].blk0 = total;  // sentinel
+    B->tab[n] = B->tab[n - 1];
+    B->tab[n].blk0 = total;  // sentinel
     B->total = total;
     B->max_pos = mp;
-    CO_CK(cudaMemcpy(B->d_tab, B->tab.data(), sizeof(co_bwork) * (B->n + 1),
-                     cudaMemcpyHostToDevice));
+    CO_CK(cudaMemcpyAsync(B->d_tab, B->tab.data(), sizeof(co_bwork) * (n + 1),
+                          cudaMemcpyHostToDevice, B->stream));
+    CO_CK(cudaStreamSynchronize(B->stream));
     return CO_OK;
 }
 
@@ -1375,6 +1387,8 @@ extern "C" int co_batch_create(const co_batch_instance *inst, int n, int n_quad,
             return rc;
         }
     }
+    for (int i = 0; i < n; i++)
+        if (B->N[i] > 0) B->live.push_back(i);
     if ((rc = batch_rebuild_table(B))) {
         co_batch_destroy(B);
         return rc;
@@ -1415,16 +1429,18 @@ static int batch_pre(co_batch *B, int i, const co_opts *o, double S0i, double dt
     return co_pack_landau(c, N, N, CO_PREC_FP64, o->use_gonzalez);
 }
 
+// one Picard iteration of the live instances (their O(N) stages, one batched
+// pair-sum launch, their Anderson updates)
 static int batch_iteration(co_batch *B, const co_opts *o, const double *S0, double dt,
                            const co_dev_opts &d) {
     int rc;
     std::vector<int> nred(B->n, 1);
-    for (int i = 0; i < B->n; i++)
+    for (int i : B->live)
         if ((rc = batch_pre(B, i, o, S0[i], dt, &nred[i]))) return rc;
-    if ((rc = co_pair64_batch(B->stream, B->d_tab, B->n, B->total, B->W, B->KC, B->grid,
-                              B->d_counter, B->max_pos)))
+    if ((rc = co_pair64_batch(B->stream, B->d_tab, (int)B->live.size(), B->total, B->W, B->KC,
+                              B->grid, B->d_counter, B->max_pos)))
         return rc;
-    for (int i = 0; i < B->n; i++) {
+    for (int i : B->live) {
         co_ctx *c = B->ctx[i];
         co_bufs &b = c->mb;
         int N = B->N[i];
@@ -1453,6 +1469,9 @@ static int batch_iteration(co_batch *B, const co_opts *o, const double *S0, doub
 extern "C" int co_batch_tune(co_batch *B, int *W, int *KC, int *grid, double *best_ms) {
     if (!B) return CO_ERR_ARG;
     CO_CK(cudaSetDevice(B->device));
+    B->live.clear();   // the tuner times the pair sum of every instance
+    for (int i = 0; i < B->n; i++)
+        if (B->N[i] > 0) B->live.push_back(i);
     // candidates: tile width, chunk of tile pairs, persistent blocks per SM
     const int Ws[] = {4, 8};
     const int KCs[] = {4, 16};
@@ -1471,8 +1490,8 @@ extern "C" int co_batch_tune(co_batch *B, int *W, int *KC, int *grid, double *be
                 int rc = batch_rebuild_table(B);
                 if (rc) return rc;
                 CO_CK(cudaEventRecord(e0, B->stream));
-                rc = co_pair64_batch(B->stream, B->d_tab, B->n, B->total, B->W, B->KC, B->grid,
-                                     B->d_counter, B->max_pos);
+                rc = co_pair64_batch(B->stream, B->d_tab, (int)B->live.size(), B->total, B->W,
+                                     B->KC, B->grid, B->d_counter, B->max_pos);
                 if (rc) return rc;
                 CO_CK(cudaEventRecord(e1, B->stream));
                 CO_CK(cudaEventSynchronize(e1));
@@ -1522,6 +1541,9 @@ extern "C" int co_batch_step_dev(co_batch *B, const co_opts *o, double *v1_all,
         k_state_reset<<<1, 32, 0, B->stream>>>(c->st);
     }
     co_dev_opts d = dev_opts(o, 0.0);
+    B->live.clear();
+    for (int i = 0; i < B->n; i++)
+        if (B->N[i] > 0) B->live.push_back(i);
     if (!B->tuned) {
         // pack every instance once at the initial guess, then time the candidates
         std::vector<int> nred(B->n);
@@ -1529,22 +1551,33 @@ extern "C" int co_batch_step_dev(co_batch *B, const co_opts *o, double *v1_all,
             if (B->model[i] == CO_MODEL_LANDAU)
                 if ((rc = batch_pre(B, i, o, S0[i], dt, &nred[i]))) return rc;
         if ((rc = co_batch_tune(B, nullptr, nullptr, nullptr, nullptr))) return rc;
+    } else if ((rc = batch_rebuild_table(B))) {
+        return rc;
     }
+    // the iteration of the live instances as a CUDA graph, re-captured whenever
+    // the live set shrinks (finished instances then cost nothing per iteration)
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;
-    if (use_graph) {
+    auto capture = [&]() -> int {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
         CO_CK(cudaStreamSynchronize(B->stream));
         CO_CK(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
-        rc = batch_iteration(B, o, S0, dt, d);
+        int r = batch_iteration(B, o, S0, dt, d);
         cudaError_t ce = cudaStreamEndCapture(B->stream, &graph);
-        if (rc) return rc;
+        if (r) return r;
         if (ce != cudaSuccess) return CO_ERR_CUDA;
-        if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
-            cudaGraphDestroy(graph);
-            return CO_ERR_CUDA;
-        }
+        if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) return CO_ERR_CUDA;
+        return CO_OK;
+    };
+    if (use_graph && (rc = capture())) {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
     }
-    int k, all_done = 0;
+    int k;
     for (k = 1; k <= o->max_iter; k++) {
         if (use_graph) {
             if (cudaGraphLaunch(exec, B->stream) != cudaSuccess) {
@@ -1560,12 +1593,17 @@ extern "C" int co_batch_step_dev(co_batch *B, const co_opts *o, double *v1_all,
             rc = CO_ERR_CUDA;
             break;
         }
-        all_done = 1;
-        for (int i = 0; i < B->n; i++) {
+        std::vector<int> still;
+        for (int i : B->live) {
             if (B->st_host[i].error) rc = B->st_host[i].error;
-            if (!B->st_host[i].finished && B->N[i] > 0) all_done = 0;
+            if (!B->st_host[i].finished) still.push_back(i);
         }
-        if (rc || all_done) break;
+        if (rc || still.empty()) break;
+        if (still.size() < B->live.size()) {
+            B->live.swap(still);
+            if ((rc = batch_rebuild_table(B))) break;
+            if (use_graph && (rc = capture())) break;
+        }
     }
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
@@ -1664,30 +1702,65 @@ __global__ void k_ws_apply(int N, const double *__restrict__ vp, const float *__
     v1[N + a] = vp[N + a] + dt2 * ((double)Y[2 * (size_t)a + 1] * s1 + h1);
 }
 
+// The warm start compares first residuals (order 1 against tol ~1e-10): the
+// mixed forms take them on the FP32 pair map.
+static int ws_prec(int precision) {
+    return precision == CO_PREC_FP64 ? CO_PREC_FP64 : CO_PREC_MIXED;
+}
+
 extern "C" int co_warmstart_features_dev(co_ctx *c, const co_opts *o, const double *v,
-                                         const double *w, int N, double dt, double *v_pred,
-                                         float *X) {
+                                         const double *w, int N, double S0, double dt,
+                                         double *v_pred, float *X, double *res_pred) {
     if (!c || !o || N < 0 || (N > 0 && (!v || !w || !v_pred || !X))) return CO_ERR_ARG;
     CO_CK(cudaSetDevice(c->device));
     int rc;
     if ((rc = co_ensure_capacity(c, N, 1))) return rc;
+    if (res_pred) *res_pred = 0.0;
     if (N == 0) return CO_OK;
     co_bufs &b = c->mb;
+    if (!b.pc && cudaMalloc(&b.pc, 7 * sizeof(double) * b.cap) != cudaSuccess) return CO_ERR_NOMEM;
+    if (!b.Adef && cudaMalloc(&b.Adef, 3 * sizeof(double) * b.cap) != cudaSuccess)
+        return CO_ERR_NOMEM;
+    double *H = b.pc + 4 * (size_t)b.cap;   // 3N: the Hessian of L at v
     CO_CK(cudaMemcpyAsync(b.v0, v, 2 * (size_t)N * sizeof(double), cudaMemcpyDeviceToDevice,
                           c->stream));
     CO_CK(cudaMemcpyAsync(b.w, w, (size_t)N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
-    if ((rc = co_predictor_buffers(c, o, o->precision, b.v0, N, dt, b.v1))) return rc;
+    const int pp = ws_prec(o->precision);
+    if ((rc = co_predictor_buffers(c, o, pp, b.v0, N, dt, b.v1))) return rc;
     if (o->model == CO_MODEL_LB) {
         // dotv of the LB predictor: (v1 - v)/dt is what Gv holds; use it directly
         k_dotv_from<<<co_cdiv(2LL * N, 256), 256, 0, c->stream>>>(2 * N, b.v1, b.v0, 1.0 / dt,
                                                                   b.dotv);
         c->launches++;
+        // no entropy potential L in the LB map: no Hessian and no pair metric
+        CO_CK(cudaMemsetAsync(H, 0, 3 * (size_t)N * sizeof(double), c->stream));
+        CO_CK(cudaMemsetAsync(b.Adef, 0, 3 * (size_t)N * sizeof(double), c->stream));
+    } else {
+        // the local stiffness factors at v (v's sort, L and G are still current):
+        // the Hessian of L and the FP32 pair metric A
+        if ((rc = co_hess_L_dev(c, N, H))) return rc;
+        if ((rc = co_pack_plain(c, N, N, CO_PREC_MIXED, b.v0, b.G))) return rc;
+        if ((rc = co_metric32(c, N))) return rc;
+        if ((rc = co_unpack_A(c, N, b.Adef))) return rc;
     }
-    if ((rc = co_features_dev(c, b.v0, N, X))) return rc;
+    if ((rc = co_features_dev(c, N, H, b.Adef, X))) return rc;
+    // the predictor's first residual r = G(v_pred) - v_pred, per marker and its norm
+    int nred = 0;
+    if ((rc = picard_map_impl(c, o->model, o->use_gonzalez, o->nu, pp, b.Gv, b.v1, b.v0, N, S0, dt,
+                              b.r, &nred)))
+        return rc;
+    if ((rc = co_features_res_dev(c, N, b.r, dt, X))) return rc;
+    co_dev_opts d = dev_opts(o, 0.0);
+    k_state_reset<<<1, 32, 0, c->stream>>>(c->st);
+    k_ctrl1<<<1, 256, 0, c->stream>>>(b.red, nred, c->st, d);
+    c->launches += 2;
     CO_CK(cudaMemcpyAsync(v_pred, b.v1, 2 * (size_t)N * sizeof(double), cudaMemcpyDeviceToDevice,
                           c->stream));
+    CO_CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(co_solver_state), cudaMemcpyDeviceToHost,
+                          c->stream));
     CO_CK(cudaStreamSynchronize(c->stream));
-    return CO_OK;
+    if (res_pred) *res_pred = c->st_host->nrm_r;
+    return c->st_host->error ? c->st_host->error : CO_OK;
 }
 
 extern "C" int co_warmstart_apply_dev(co_ctx *c, const double *v_pred, const float *Y, int N,
@@ -1719,8 +1792,8 @@ extern "C" int co_picard_residual_dev(co_ctx *c, const co_opts *o, const double 
     CO_CK(cudaMemcpyAsync(b.v0, v0, n2, cudaMemcpyDeviceToDevice, c->stream));
     CO_CK(cudaMemcpyAsync(b.w, w, (size_t)N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
     int nred = 0;
-    if ((rc = picard_map_impl(c, o->model, o->use_gonzalez, o->nu, o->precision, b.Gv, b.vin, b.v0,
-                              N, S0, dt, b.r, &nred)))
+    if ((rc = picard_map_impl(c, o->model, o->use_gonzalez, o->nu, ws_prec(o->precision), b.Gv,
+                              b.vin, b.v0, N, S0, dt, b.r, &nred)))
         return rc;
     co_dev_opts d = dev_opts(o, 0.0);
     k_state_reset<<<1, 32, 0, c->stream>>>(c->st);

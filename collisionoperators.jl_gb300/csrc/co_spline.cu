@@ -488,14 +488,19 @@ __global__ void k_hess_L(int N, const int *__restrict__ cell, const double *__re
     H[2 * (size_t)N + a] = h22;
 }
 
-// Warm-start features per marker (after the predictor at x): v, G (entropy
-// gradient), vdot (predictor velocity), log max(f_s, 1e-30) and the clamped
-// grad f_s / f_s, as FP32 rows of 9.
-__global__ void k_features(const double *__restrict__ x, int N, const int *__restrict__ cell,
-                           const double *__restrict__ xi, const double *__restrict__ fc, int n1,
-                           int nd1, const double *__restrict__ bp1, const double *__restrict__ bp2,
+// Warm-start features per marker at the step's start x (after the predictor),
+// FP32 rows of CO_WS_NFEAT: 0-1 the predictor velocity vdot, 2-3 G (entropy
+// gradient), 4-5 the clamped grad f_s / f_s, 6 log max(f_s, 1e-30), 7-9 the
+// Hessian of L (H11, H12, H22), 10-12 the FP32 pair metric A (A11, A12, A22);
+// columns 13-14 (the predictor's first residual / dt) are written afterwards.
+// H and A are the two factors of the local stiffness dt A H / 2 of the implicit
+// step, so the network sees the quantities a local Newton correction needs.
+__global__ void k_features(int N, const int *__restrict__ cell, const double *__restrict__ xi,
+                           const double *__restrict__ fc, int n1, int nd1,
+                           const double *__restrict__ bp1, const double *__restrict__ bp2,
                            const double *__restrict__ C1, const double *__restrict__ C2,
                            const double *__restrict__ G, const double *__restrict__ vdot,
+                           const double *__restrict__ H, const double *__restrict__ A,
                            float *__restrict__ X) {
     int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= N) return;
@@ -523,16 +528,27 @@ __global__ void k_features(const double *__restrict__ x, int N, const int *__res
         g1 = fmin(fmax(d1 * invf, -CO_G_MAX), CO_G_MAX);
         g2 = fmin(fmax(d2 * invf, -CO_G_MAX), CO_G_MAX);
     }
-    float *o = X + (size_t)a * 9;
-    o[0] = (float)x[a];
-    o[1] = (float)x[N + a];
+    float *o = X + (size_t)a * CO_WS_NFEAT;
+    o[0] = (float)vdot[a];
+    o[1] = (float)vdot[N + a];
     o[2] = (float)G[a];
     o[3] = (float)G[N + a];
-    o[4] = (float)vdot[a];
-    o[5] = (float)vdot[N + a];
+    o[4] = (float)g1;
+    o[5] = (float)g2;
     o[6] = (float)log(fmax(f, CO_FS_FLOOR));
-    o[7] = (float)g1;
-    o[8] = (float)g2;
+    for (int k = 0; k < 3; k++) {
+        o[7 + k] = (float)H[(size_t)k * N + a];
+        o[10 + k] = (float)A[(size_t)k * N + a];
+    }
+}
+
+// columns 13-14 of the features: the predictor's first residual r / dt
+__global__ void k_features_res(int N, const double *__restrict__ r, double inv_dt,
+                               float *__restrict__ X) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= N) return;
+    X[(size_t)a * CO_WS_NFEAT + 13] = (float)(r[a] * inv_dt);
+    X[(size_t)a * CO_WS_NFEAT + 14] = (float)(r[N + a] * inv_dt);
 }
 
 // ---------------------------------------------------------------- host side
@@ -734,12 +750,21 @@ int co_hess_L_dev(co_ctx *c, int N, double *H) {
     return CO_OK;
 }
 
-// features at x (cell/xi of x's last sort, coefficients in c->f)
-int co_features_dev(co_ctx *c, const double *x, int N, float *X) {
+// features at the last sorted markers (cell/xi of that sort, coefficients in
+// c->f, G and dotv in the marker buffers, H and A as given)
+int co_features_dev(co_ctx *c, int N, const double *H, const double *A, float *X) {
     if (N == 0) return CO_OK;
-    k_features<<<co_cdiv(N, 256), 256, 0, c->stream>>>(x, N, c->mb.cell, c->mb.xi, c->f, c->n1,
+    k_features<<<co_cdiv(N, 256), 256, 0, c->stream>>>(N, c->mb.cell, c->mb.xi, c->f, c->n1,
                                                        c->nd1, c->bp1, c->bp2, c->C1, c->C2,
-                                                       c->mb.G, c->mb.dotv, X);
+                                                       c->mb.G, c->mb.dotv, H, A, X);
+    c->launches++;
+    CO_CK(cudaGetLastError());
+    return CO_OK;
+}
+
+int co_features_res_dev(co_ctx *c, int N, const double *r, double dt, float *X) {
+    if (N == 0) return CO_OK;
+    k_features_res<<<co_cdiv(N, 256), 256, 0, c->stream>>>(N, r, 1.0 / dt, X);
     c->launches++;
     CO_CK(cudaGetLastError());
     return CO_OK;

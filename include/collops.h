@@ -278,16 +278,24 @@ int co_mlp_gradients(co_mlp *mlp, const float *X, const float *T, int B, float *
 int co_mlp_train_step(co_mlp *mlp, const float *X, const float *T, int B, float lr,
                       float *loss);
 /* Per-marker features of the warm start at the start of a step (device
- * pointers): runs the explicit predictor, writing v_pred, and fills X (N x 9,
- * row-major): v1, v2, G1, G2 (entropy gradient), vdot1, vdot2 (predictor
- * velocity), log max(f_s, 1e-30), and grad f_s / f_s (clamped as LOGGRAD_FN). */
+ * pointers): runs the explicit predictor, writing v_pred, and fills X (N x 15,
+ * row-major FP32): vdot1, vdot2 (predictor velocity), G1, G2 (entropy
+ * gradient), grad f_s / f_s (clamped as LOGGRAD_FN), log max(f_s, 1e-30), the
+ * Hessian of L (H11, H12, H22), the FP32 pair metric A (A11, A12, A22; H and A
+ * are 0 for LB), and the predictor's first residual (G(v_pred) - v_pred) / dt;
+ * res_pred (may be NULL) receives ||G(v_pred) - v_pred||. The mixed forms run
+ * the predictor and the residual map on the FP32 pair sum. S0 is the entropy of
+ * v's projection (for the Gonzalez correction of the residual map). */
 int co_warmstart_features_dev(co_ctx *ctx, const co_opts *opts, const double *v,
-                              const double *w, int N, double dt, double *v_pred, float *X);
+                              const double *w, int N, double S0, double dt, double *v_pred,
+                              float *X, double *res_pred);
 /* v1 = v_pred + dt^2 (Y * scale + shift) per component (device pointers). */
 int co_warmstart_apply_dev(co_ctx *ctx, const double *v_pred, const float *Y, int N,
                            double dt, const double *scale2, const double *shift2,
                            double *v1);
-/* ||G(v_in) - v_in|| of one Picard map at opts->precision (device pointers). */
+/* ||G(v_in) - v_in|| of one Picard map (device pointers): FP64 pair sum for
+ * CO_PREC_FP64, the FP32 pair sum for the mixed forms (a first-residual
+ * comparison at the warm-start level). */
 int co_picard_residual_dev(co_ctx *ctx, const co_opts *opts, const double *v_in,
                            const double *v0, const double *w, int N, double S0, double dt,
                            double *res);

@@ -79,7 +79,7 @@ def test_learned_warm_start_small(built_lib, collops_mod, tmp_path):
                            "step")
         return it.value
     X, T, x = learned.generate_pairs(ws, o, vd, wd, dt, 6, solve)
-    assert X.shape == (6 * 2048, 9) and np.all(np.isfinite(X)) and np.all(np.isfinite(T))
+    assert X.shape == (6 * 2048, learned.N_IN) and np.all(np.isfinite(X)) and np.all(np.isfinite(T))
     wsn = learned.WarmStart()
     hist = wsn.fit(X, T, epochs=30, batch=1024, lr=2e-3)
     assert hist[-1] < hist[0]
@@ -91,8 +91,7 @@ def test_learned_warm_start_small(built_lib, collops_mod, tmp_path):
     used, rl, rp = wsn2.propose(ws, o, x, wd, S0, dt, v1)
     assert np.isfinite(rl) and np.isfinite(rp)
     it_learned = solve(v1.clone(), x, S0)
-    vp = torch.empty_like(x)
-    Xf, vp = learned.features(ws, o, x, wd, dt)
+    Xf, vp, _rp = learned.features(ws, o, x, wd, S0, dt)
     it_plain = solve(vp.clone(), x, S0)
     print(f"learned warm start: used={used} r_learned={rl:.3e} r_predictor={rp:.3e} "
           f"iterations learned-start={it_learned} predictor-start={it_plain}")
@@ -129,7 +128,7 @@ def test_trained_warm_start_gain(built_lib, collops_mod):
         S0 = learned.entropy_of(ws, x, wd)
         v1 = torch.empty_like(x)
         used, rl, rp = warm.propose(ws, o, x, wd, S0, dt, v1)
-        _X, vp = learned.features(ws, o, x, wd, dt)
+        _X, vp, _rp = learned.features(ws, o, x, wd, S0, dt)
         its = []
         for start in (v1.clone(), vp.clone()):
             it, inner = C.c_int(), C.c_int()
