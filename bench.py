@@ -263,7 +263,7 @@ def run_gpu(args, cfg):
         if not os.path.exists(args.warmstart_file):
             raise SystemExit(f"warm-start weights not found: {args.warmstart_file}")
         warm = learned.WarmStart.load(args.warmstart_file, device=local)
-    ws_stats = {"used": 0, "steps": 0, "mlp_launches": 0}
+    ws_stats = {"used": 0, "steps": 0, "mlp_launches": 0, "retries": 0}
 
     def initial_guess(x, S0, prec, learned_start):
         """v1 <- the warm start of the step from x: the learned proposal (kept only
@@ -297,10 +297,22 @@ def run_gpu(args, cfg):
         return (it.value, res.value, nrs.value, r0.value)
 
     def one_step(x, S0, prec, solver=None, learned_start=True):
-        """warm start + implicit solve + S of the new state; returns (x1, S1, info)."""
+        """warm start + implicit solve + S of the new state; returns (x1, S1, info).
+        The headline form (learned start, defect correction) retries a stagnated
+        solve once from the other start candidate (collops.learned.step_defect_warm)."""
         solver = solver or args.solver
-        initial_guess(x, S0, prec, learned_start and solver == args.solver and prec == args.form)
-        info = solve(x, S0, prec, solver)
+        headline = learned_start and solver == args.solver and prec == args.form
+        if headline and warm is not None and solver == "defect":
+            o = opts(prec)
+            o.stag_rel_tol = 0.1
+            info, rec = learned.step_defect_warm(ws, warm, o, dopt, x, w, S0, dt, v1)
+            ws_stats["used"] += int(rec["used_learned"])
+            ws_stats["steps"] += 1
+            ws_stats["mlp_launches"] += 1
+            ws_stats["retries"] += rec["attempts"] - 1
+        else:
+            initial_guess(x, S0, prec, headline)
+            info = solve(x, S0, prec, solver)
         S1 = entropy(v1)
         return v1.clone(), S1, info
 
@@ -536,7 +548,10 @@ def run_gpu(args, cfg):
         "plain_fp64": plain, "accuracy": acc,
         "warmstart": ({"kind": "learned MLP (BF16, own kernels)", "file": os.path.relpath(
             args.warmstart_file, ROOT), "learned_start_used": ws_stats["used"],
-            "steps": ws_stats["steps"]} if warm is not None else {"kind": "explicit predictor"}),
+            "steps": ws_stats["steps"], "retries_from_other_start": ws_stats["retries"],
+            "rule": "learned proposal when its first residual is below the predictor's; a "
+                    "stagnated solve is repeated once from the other start"}
+            if warm is not None else {"kind": "explicit predictor"}),
         "roofline": dominant, "roofline_fp64": r64, "roofline_fp32": r32, "roofline_ds": rds,
         "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": int(n_launch),
     }

@@ -63,13 +63,30 @@ class MLP:
         _check(self.lib.co_mlp_set_params(self.h, p.ctypes.data_as(C.POINTER(C.c_float))),
                "co_mlp_set_params")
 
+    def _rows(self, X, cols: int, name: str) -> int:
+        """The kernels take row pointers and a row count only: check the layout
+        (contiguous float32 CUDA rows of exactly `cols`) before every call."""
+        import torch
+        if not (isinstance(X, torch.Tensor) and X.is_cuda and X.dtype == torch.float32 and
+                X.dim() == 2 and X.shape[1] == cols and X.is_contiguous()):
+            raise CollopsError(f"{name}: expected a contiguous float32 CUDA tensor (B, {cols}), "
+                               f"got {getattr(X, 'shape', None)} "
+                               f"{getattr(X, 'dtype', type(X).__name__)}")
+        return X.shape[0]
+
     def forward(self, X, Y, stream: int = 0) -> None:
         """X (B, n_in) and Y (B, n_out): float32 CUDA tensors; enqueued on `stream`
         (a cudaStream_t as an int, 0 = the legacy default stream)."""
-        _check(self.lib.co_mlp_forward(self.h, X.data_ptr(), X.shape[0], Y.data_ptr(),
+        B = self._rows(X, self.n_in, "X")
+        if self._rows(Y, self.n_out, "Y") != B:
+            raise CollopsError("forward: X and Y row counts differ")
+        _check(self.lib.co_mlp_forward(self.h, X.data_ptr(), B, Y.data_ptr(),
                                        C.c_void_p(stream or None)), "co_mlp_forward")
 
     def gradients(self, X, T):
+        B = self._rows(X, self.n_in, "X")
+        if self._rows(T, self.n_out, "T") != B:
+            raise CollopsError("gradients: X and T row counts differ")
         g = np.zeros(self.P, dtype=np.float32)
         loss = C.c_float()
         _check(self.lib.co_mlp_gradients(self.h, X.data_ptr(), T.data_ptr(), X.shape[0],
@@ -78,6 +95,9 @@ class MLP:
         return g, loss.value
 
     def train_step(self, X, T, lr: float) -> float:
+        B = self._rows(X, self.n_in, "X")
+        if self._rows(T, self.n_out, "T") != B:
+            raise CollopsError("train_step: X and T row counts differ")
         loss = C.c_float()
         _check(self.lib.co_mlp_train_step(self.h, X.data_ptr(), T.data_ptr(), X.shape[0], lr,
                                           C.byref(loss)), "co_mlp_train_step")
@@ -103,10 +123,10 @@ class WarmStart:
 
     def __init__(self, mlp: MLP | None = None, device: int = 0):
         self.mlp = mlp or MLP(device=device)
-        self.xm = np.zeros(N_IN)
-        self.xs = np.ones(N_IN)
-        self.tm = np.zeros(N_OUT)
-        self.ts = np.ones(N_OUT)
+        self.xm = np.zeros(self.mlp.n_in)
+        self.xs = np.ones(self.mlp.n_in)
+        self.tm = np.zeros(self.mlp.n_out)
+        self.ts = np.ones(self.mlp.n_out)
         self._xm_dev = self._xs_dev = None   # device copies of xm, xs
 
     def fit(self, X: np.ndarray, T: np.ndarray, epochs: int = 20, batch: int = 8192,
@@ -147,10 +167,12 @@ class WarmStart:
             self.mlp.forward(Xn, Y, stream)
         return Y
 
-    def propose(self, ws: Workspace, opts: CoOpts, v, w, S0: float, dt: float, v1_out):
+    def propose(self, ws: Workspace, opts: CoOpts, v, w, S0: float, dt: float, v1_out,
+                alt_out=None):
         """Fill v1_out with the initial iterate: the learned proposal if its first
-        residual is smaller than the predictor's, else the predictor. Returns
-        (used_learned, residual_learned, residual_predictor)."""
+        residual is smaller than the predictor's, else the predictor (and alt_out,
+        if given, with the other one). Returns (used_learned, residual_learned,
+        residual_predictor)."""
         import torch
         X, vp, rp_pred = features(ws, opts, v, w, S0, dt)
         # features() returns after the context stream has drained; the network and
@@ -169,6 +191,8 @@ class WarmStart:
         use = rl.value < rp_pred
         with torch.cuda.stream(torch.cuda.ExternalStream(ws.stream(), device=v.device)):
             v1_out.copy_(vl if use else vp)
+            if alt_out is not None:
+                alt_out.copy_(vp if use else vl)
         return use, rl.value, rp_pred
 
     def save(self, path: str) -> None:
@@ -179,10 +203,52 @@ class WarmStart:
     def load(cls, path: str, device: int = 0) -> "WarmStart":
         z = np.load(path)
         ws = cls(device=device)
+        if z["params"].size != ws.mlp.P or z["xm"].size != ws.mlp.n_in:
+            raise CollopsError(f"{path}: {z['xm'].size}-feature network, this library builds "
+                               f"{ws.mlp.n_in} features per marker; retrain with "
+                               "collops.train_warmstart")
         ws.mlp.set_params(z["params"])
         ws.xm, ws.xs, ws.tm, ws.ts = z["xm"], z["xs"], z["tm"], z["ts"]
         ws._xm_dev = None
         return ws
+
+
+def step_defect_warm(ws: Workspace, warm: "WarmStart", opts: CoOpts, dopt, x, w, S0: float,
+                     dt: float, v1, retry: bool = True):
+    """One implicit step from x (torch (2, N)) by defect correction
+    (co_step_defect_dev) started from the learned warm start. When the solve
+    from the chosen start stagnates above the tolerance, it is solved once more
+    from the other candidate (predictor or learned proposal) and the better of
+    the two results is kept. v1 receives the new markers. Returns
+    (outer, residual, inner, r0) of the kept solve and a record of the
+    proposal and the attempts."""
+    import torch
+    alt = torch.empty_like(x)
+    used, rl, rp = warm.propose(ws, opts, x, w, S0, dt, v1, alt)
+    N = x.shape[1]
+
+    def solve(start):
+        it, inner = C.c_int(), C.c_int()
+        res, r0 = C.c_double(), C.c_double()
+        _check(ws.lib.co_step_defect_dev(ws.h, C.byref(opts), C.byref(dopt), start.data_ptr(),
+                                         x.data_ptr(), w.data_ptr(), N, S0, dt, C.byref(it),
+                                         C.byref(res), C.byref(inner), C.byref(r0)),
+               "co_step_defect_dev")
+        return (it.value, res.value, inner.value, r0.value)
+
+    info = solve(v1)
+    rec = dict(used_learned=bool(used), r_learned=rl, r_predictor=rp, attempts=1)
+    if retry and not info[1] < opts.tol * float(torch.linalg.vector_norm(v1)):
+        info2 = solve(alt)
+        rec["attempts"] = 2
+        if info2[1] < info[1]:
+            v1.copy_(alt)
+            info = (info[0] + info2[0], info2[1], info[2] + info2[2], info[3])
+            rec["kept"] = "retry"
+        else:
+            info = (info[0] + info2[0], info[1], info[2] + info2[2], info[3])
+            rec["kept"] = "first"
+    return info, rec
 
 
 def generate_pairs(ws: Workspace, opts: CoOpts, v, w, dt: float, steps: int, solve):

@@ -20,7 +20,7 @@ def test_mlp_forward_and_gradients_match_oracle(built_lib, collops_mod):
     import torch
     from collops import learned
     from oracle import mlp as om
-    net = learned.MLP(seed=3)
+    net = learned.MLP(seed=3, n_in=9)
     p = net.get_params()
     rng = np.random.default_rng(1)
     X = rng.standard_normal((1000, 9)).astype(np.float32)
@@ -44,7 +44,7 @@ def test_mlp_training_reduces_loss(built_lib, collops_mod):
     X = rng.standard_normal((16384, 9)).astype(np.float32)
     W = rng.standard_normal((9, 2)).astype(np.float32)
     T = np.tanh(X @ W).astype(np.float32)
-    ws = learned.WarmStart()
+    ws = learned.WarmStart(mlp=learned.MLP(n_in=9))
     hist = ws.fit(X, T, epochs=12, batch=2048, lr=3e-3)
     ws.mlp.close()
     assert hist[-1] < 0.2 * hist[0]
@@ -147,3 +147,33 @@ def test_trained_warm_start_gain(built_lib, collops_mod):
         gains.append(rp / rl)
     warm.mlp.close()
     assert min(gains) > 1.25
+
+
+def test_step_defect_warm(built_lib, collops_mod):
+    """The learned-start step helper: proposal, defect-correction solve (retry from
+    the other start only on stagnation), result a converged step that conserves
+    momentum and energy."""
+    import torch
+    from collops import learned
+    warm = learned.WarmStart.load(os.path.join(PKG, "collops", "warmstart_c3.npz"))
+    N, n = 16384, 32
+    bp = uniform_bp(-6.0, 6.0, n)
+    v, w = gaussian_markers(N, 0.9, 0.6, seed=503)
+    p = collops_mod.SimParameters(bp1=bp, bp2=bp, m_anderson=8, damping=0.7, tol=1e-12,
+                                  abs_floor=0.0, max_iter=400, precision="mixed_ds")
+    ws = collops_mod.build_workspace(p)
+    o = p.opts()
+    o.stag_rel_tol = 0.1
+    x = torch.from_numpy(np.ascontiguousarray(v.T)).cuda()
+    wd = torch.from_numpy(w).cuda()
+    S0 = learned.entropy_of(ws, x, wd)
+    v1 = torch.empty_like(x)
+    d = collops_mod.CoDefectOpts(0.05, 60, 5, 0.5, 0, 0, 0, 1e-2)
+    info, rec = learned.step_defect_warm(ws, warm, o, d, x, wd, S0, 0.02, v1)
+    ws.close()
+    warm.mlp.close()
+    x1 = v1.cpu().numpy().T
+    assert rec["attempts"] in (1, 2) and info[1] < 1e-12 * np.linalg.norm(x1)
+    assert np.max(np.abs((w[:, None] * (x1 - v)).sum(0))) < 1e-12
+    E0 = 0.5 * np.sum(w * (v ** 2).sum(1))
+    assert abs(0.5 * np.sum(w * (x1 ** 2).sum(1)) - E0) < 1e-12 * E0
