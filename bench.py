@@ -254,7 +254,7 @@ def run_gpu(args, cfg):
                   "co_entropy_of_markers_dev")
         return S.value
 
-    dopt = co.CoDefectOpts(args.dc_eta, args.dc_max_inner, args.dc_stag_window, 0.5, 0,
+    dopt = co.CoDefectOpts(args.dc_eta, args.dc_max_inner, args.dc_stag_window, args.dc_fp32_stall, 0,
                            args.dc_outer_m, args.dc_precond, args.dc_metric_freeze)
 
     warm = None
@@ -665,6 +665,9 @@ def main(argv=None):
     ap.add_argument("--dc-eta", type=float, default=0.05)
     ap.add_argument("--dc-max-inner", type=int, default=60)
     ap.add_argument("--dc-stag-window", type=int, default=5)
+    ap.add_argument("--dc-fp32-stall", type=float, default=0.5,
+                    help="the mixed forms leave FP32 outer maps once a map cuts the residual "
+                         "by less than this factor")
     ap.add_argument("--dc-outer-m", type=int, default=0,
                     help="Anderson depth over the defect correction's outer iterates")
     ap.add_argument("--dc-precond", type=int, default=0, choices=[0, 1, 2],

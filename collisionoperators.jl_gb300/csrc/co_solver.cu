@@ -1272,6 +1272,11 @@ struct co_batch {
     unsigned *d_counter;
     int total, max_pos;
     std::vector<int> live;            // instances still iterating (table and graph cover these)
+    // the O(N) stages of different instances are independent: an iteration forks
+    // them over aux streams (joined around the batched pair launch)
+    std::vector<cudaStream_t> aux;
+    std::vector<cudaEvent_t> ev_join1, ev_join2;
+    cudaEvent_t ev_fork1, ev_fork2;
     int W, KC, grid, tuned;
     double tune_ms;
     int nsm;
@@ -1347,6 +1352,26 @@ extern "C" int co_batch_create(const co_batch_instance *inst, int n, int n_quad,
         delete B;
         return CO_ERR_CUDA;
     }
+    B->ev_fork1 = B->ev_fork2 = nullptr;
+    {
+        const int n_aux = n < 8 ? n : 8;
+        bool ok = cudaEventCreateWithFlags(&B->ev_fork1, cudaEventDisableTiming) == cudaSuccess &&
+                  cudaEventCreateWithFlags(&B->ev_fork2, cudaEventDisableTiming) == cudaSuccess;
+        for (int j = 0; ok && j < n_aux; j++) {
+            cudaStream_t st;
+            cudaEvent_t e1, e2;
+            ok = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess;
+            if (ok) B->aux.push_back(st);
+            ok = ok && cudaEventCreateWithFlags(&e1, cudaEventDisableTiming) == cudaSuccess;
+            if (ok) B->ev_join1.push_back(e1);
+            ok = ok && cudaEventCreateWithFlags(&e2, cudaEventDisableTiming) == cudaSuccess;
+            if (ok) B->ev_join2.push_back(e2);
+        }
+        if (!ok) {
+            co_batch_destroy(B);
+            return CO_ERR_CUDA;
+        }
+    }
     if (cudaMalloc(&B->st_all, sizeof(co_solver_state) * n) != cudaSuccess ||
         cudaMallocHost(&B->st_host, sizeof(co_solver_state) * n) != cudaSuccess ||
         cudaMalloc(&B->d_tab, sizeof(co_bwork) * (n + 1)) != cudaSuccess ||
@@ -1410,6 +1435,11 @@ extern "C" int co_batch_destroy(co_batch *B) {
     if (B->st_host) cudaFreeHost(B->st_host);
     if (B->d_tab) cudaFree(B->d_tab);
     if (B->d_counter) cudaFree(B->d_counter);
+    for (cudaStream_t st : B->aux) cudaStreamDestroy(st);
+    for (cudaEvent_t e : B->ev_join1) cudaEventDestroy(e);
+    for (cudaEvent_t e : B->ev_join2) cudaEventDestroy(e);
+    if (B->ev_fork1) cudaEventDestroy(B->ev_fork1);
+    if (B->ev_fork2) cudaEventDestroy(B->ev_fork2);
     if (B->stream) cudaStreamDestroy(B->stream);
     delete B;
     return CO_OK;
@@ -1429,17 +1459,40 @@ static int batch_pre(co_batch *B, int i, const co_opts *o, double S0i, double dt
     return co_pack_landau(c, N, N, CO_PREC_FP64, o->use_gonzalez);
 }
 
-// one Picard iteration of the live instances (their O(N) stages, one batched
-// pair-sum launch, their Anderson updates)
-static int batch_iteration(co_batch *B, const co_opts *o, const double *S0, double dt,
-                           const co_dev_opts &d) {
+// fork: every aux stream waits for the main stream's work so far
+static int batch_fork(co_batch *B, cudaEvent_t ev) {
+    CO_CK(cudaEventRecord(ev, B->stream));
+    for (cudaStream_t st : B->aux) CO_CK(cudaStreamWaitEvent(st, ev, 0));
+    return CO_OK;
+}
+// join: the main stream waits for every aux stream
+static int batch_join(co_batch *B, std::vector<cudaEvent_t> &ev) {
+    for (size_t j = 0; j < B->aux.size(); j++) {
+        CO_CK(cudaEventRecord(ev[j], B->aux[j]));
+        CO_CK(cudaStreamWaitEvent(B->stream, ev[j], 0));
+    }
+    return CO_OK;
+}
+
+// one Picard iteration of the live instances: their O(N) stages (instance j of
+// the live set on aux stream j mod K), one batched pair-sum launch on the main
+// stream, their Anderson updates (aux streams again)
+static int batch_iteration_impl(co_batch *B, const co_opts *o, const double *S0, double dt,
+                                const co_dev_opts &d) {
     int rc;
     std::vector<int> nred(B->n, 1);
-    for (int i : B->live)
+    const size_t K = B->aux.size();
+    if ((rc = batch_fork(B, B->ev_fork1))) return rc;
+    for (size_t j = 0; j < B->live.size(); j++) {
+        const int i = B->live[j];
+        B->ctx[i]->stream = B->aux[j % K];
         if ((rc = batch_pre(B, i, o, S0[i], dt, &nred[i]))) return rc;
+    }
+    if ((rc = batch_join(B, B->ev_join1))) return rc;
     if ((rc = co_pair64_batch(B->stream, B->d_tab, (int)B->live.size(), B->total, B->W, B->KC,
                               B->grid, B->d_counter, B->max_pos)))
         return rc;
+    if ((rc = batch_fork(B, B->ev_fork2))) return rc;
     for (int i : B->live) {
         co_ctx *c = B->ctx[i];
         co_bufs &b = c->mb;
@@ -1449,21 +1502,29 @@ static int batch_iteration(co_batch *B, const co_opts *o, const double *S0, doub
             if ((rc = co_unpack_update(c, N, dt, b.Gv, b.v0, b.v1, b.r, b.red))) return rc;
         int n2 = 2 * N, eg = ew_grid(c, n2);
         size_t ldF = 2 * (size_t)b.cap;
-        k_ctrl1<<<1, 256, 0, B->stream>>>(b.red, nred[i], c->st, d);
-        k_plain_update<<<eg, 256, 0, B->stream>>>(n2, c->st, o->exit_picard_step, b.v1, b.Gv, b.r,
-                                                  b.rp, b.Gp, b.vbest);
+        cudaStream_t cs = c->stream;
+        k_ctrl1<<<1, 256, 0, cs>>>(b.red, nred[i], c->st, d);
+        k_plain_update<<<eg, 256, 0, cs>>>(n2, c->st, o->exit_picard_step, b.v1, b.Gv, b.r, b.rp,
+                                           b.Gp, b.vbest);
         int ng = red_blocks(c, n2);
-        k_anderson_cols<<<ng, CO_RED_THREADS, 0, B->stream>>>(n2, c->st, b.r, b.rp, b.Gv, b.Gp,
-                                                              b.dF, b.dG, ldF, b.red);
-        k_anderson_solve<<<1, 256, 0, B->stream>>>(b.red, ng, c->st, d);
-        k_anderson_update<<<eg, 256, 0, B->stream>>>(n2, c->st, b.v1, b.Gv, b.dG, ldF);
-        k_finish_once<<<eg, 256, 0, B->stream>>>(n2, c->st, o->exit_picard_step, b.v1, b.Gv,
-                                                 b.vbest);
-        k_mark_finished<<<1, 32, 0, B->stream>>>(c->st);
+        k_anderson_cols<<<ng, CO_RED_THREADS, 0, cs>>>(n2, c->st, b.r, b.rp, b.Gv, b.Gp, b.dF,
+                                                       b.dG, ldF, b.red);
+        k_anderson_solve<<<1, 256, 0, cs>>>(b.red, ng, c->st, d);
+        k_anderson_update<<<eg, 256, 0, cs>>>(n2, c->st, b.v1, b.Gv, b.dG, ldF);
+        k_finish_once<<<eg, 256, 0, cs>>>(n2, c->st, o->exit_picard_step, b.v1, b.Gv, b.vbest);
+        k_mark_finished<<<1, 32, 0, cs>>>(c->st);
         c->launches += 7;
     }
+    if ((rc = batch_join(B, B->ev_join2))) return rc;
     CO_CK(cudaGetLastError());
     return CO_OK;
+}
+
+static int batch_iteration(co_batch *B, const co_opts *o, const double *S0, double dt,
+                           const co_dev_opts &d) {
+    int rc = batch_iteration_impl(B, o, S0, dt, d);
+    for (co_ctx *c : B->ctx) c->stream = B->stream;   // every context back on the main stream
+    return rc;
 }
 
 extern "C" int co_batch_tune(co_batch *B, int *W, int *KC, int *grid, double *best_ms) {
