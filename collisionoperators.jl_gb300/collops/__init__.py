@@ -144,6 +144,8 @@ _SIGNATURES = {
                                    C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "co_mlp_train_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_float,
                                     C.POINTER(C.c_float)]),
+    "co_diagnostics": (C.c_int, [C.c_void_p, _dp, _dp, C.c_int, _dp]),
+    "co_diagnostics_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, _dp]),
     "co_warmstart_features_dev": (C.c_int, [C.c_void_p, C.POINTER(CoOpts), C.c_void_p,
                                             C.c_void_p, C.c_int, C.c_double, C.c_double,
                                             C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
@@ -515,6 +517,18 @@ def step_defect(ws: Workspace, v1, v0, w_parts, S0: float, dt: float, *, m: int 
                                  _p(_vec(w_parts, N, "w_parts")), N, S0, dt, C.byref(it),
                                  C.byref(res), C.byref(inner), C.byref(r0)), "co_step_defect")
     return it.value, res.value, inner.value, r0.value
+
+
+def diagnostics(ws: Workspace, v_parts, w_parts) -> dict:
+    """Post-step diagnostics of main.jl:298-307 on the device: entropy, energy,
+    momentum, ||f_s - f_p||_2 and the negative-part L1 norm of f_s."""
+    v = _markers(v_parts, name="v_parts")
+    N = v.shape[0]
+    out = np.zeros(6)
+    _check(ws.lib.co_diagnostics(ws.h, _p(v), _p(_vec(w_parts, N, "w_parts")), N, _p(out)),
+           "co_diagnostics")
+    return dict(entropy=out[0], energy=out[1], momentum=(out[2], out[3]), fs_minus_fp_l2=out[4],
+                negative_part_l1=out[5])
 
 
 def predictor(ws: Workspace, v1, v_parts, w_parts, dt: float, precision: str = "fp64") -> None:

@@ -593,6 +593,36 @@ extern "C" int co_entropy_of_markers_dev(co_ctx *c, const double *v, const doubl
     return finish(c);
 }
 
+// post-step diagnostics (main.jl:298-307): out6 = {S, energy, P1, P2,
+// ||f_s - f_p||_2, negative-part L1}
+extern "C" int co_diagnostics_dev(co_ctx *c, const double *v, const double *w, int N,
+                                  double *out6) {
+    ENTER(c);
+    if (N < 0 || !out6 || (N > 0 && (!v || !w))) return CO_ERR_ARG;
+    RC(co_ensure_capacity(c, N, 1));
+    co_bufs &b = c->mb;
+    if (N > 0)
+        CO_CK(cudaMemcpyAsync(b.w, w, (size_t)N * sizeof(double), cudaMemcpyDeviceToDevice,
+                              c->stream));
+    RC(co_diagnostics_impl(c, v, N, c->y));
+    RC(d2h(c, out6, c->y, 6));
+    return finish(c);
+}
+
+extern "C" int co_diagnostics(co_ctx *c, const double *v, const double *w, int N,
+                              double *out6) {
+    ENTER(c);
+    if (N < 0 || !out6 || (N > 0 && (!v || !w))) return CO_ERR_ARG;
+    if (N > 0 && (!all_finite(v, 2 * (size_t)N) || !all_finite(w, N))) return CO_ERR_NONFINITE;
+    RC(co_ensure_capacity(c, N, 1));
+    co_bufs &b = c->mb;
+    RC(h2d(c, b.vmid, v, 2 * (size_t)N));
+    RC(h2d(c, b.w, w, N));
+    RC(co_diagnostics_impl(c, b.vmid, N, c->y));
+    RC(d2h(c, out6, c->y, 6));
+    return finish(c);
+}
+
 static int check_defect(const co_opts *o, const co_defect_opts *d) {
     int rc = check_opts(o);
     if (rc) return rc;

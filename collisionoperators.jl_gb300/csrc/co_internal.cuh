@@ -144,6 +144,7 @@ int co_loggrad_dev(co_ctx *c, const double *x, int N, const double *f, double *g
                    const double *w, const double *dv, double *red);
 int co_mid_dv(co_ctx *c, const double *vin, const double *v0, int N);
 int co_hess_L_dev(co_ctx *c, int N, double *H);
+int co_diagnostics_impl(co_ctx *c, const double *x, int N, double *out6);
 #define CO_WS_NFEAT 15   // warm-start features per marker
 int co_features_dev(co_ctx *c, int N, const double *H, const double *A, float *X);
 int co_features_res_dev(co_ctx *c, int N, const double *r, double dt, float *X);

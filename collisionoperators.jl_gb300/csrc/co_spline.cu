@@ -331,6 +331,107 @@ k_elem(const double *__restrict__ fc, int n1, int n2, int nd1, int nq,
     }
 }
 
+// Post-step diagnostics per element on the N_QUAD Gauss grid (main.jl:298-307):
+// D[e] = {entropy partial (compute_entropy, functions.jl:137-155), negative part
+// of f_s (compute_negative_part_l1, :300-313), (f_s - f_p)^2 with f_p the
+// element's marker mass over its area (compute_fs_minus_fp_l2, :315-347)}. The
+// element's marker mass is the sum of its nine cell-sum entries bS[e][k] =
+// sum_{a in e} w_a phi_k(v_a): the nine local basis functions sum to 1 there.
+__global__ void __launch_bounds__(64)
+k_diag_elem(const double *__restrict__ fc, int n1, int nd1, int nq,
+            const double *__restrict__ Tq1, const double *__restrict__ Tq2,
+            const double *__restrict__ qw, const double *__restrict__ bp1,
+            const double *__restrict__ bp2, int logsq, const double *__restrict__ bS,
+            double *__restrict__ D) {
+    __shared__ double contrib[64 * 3];
+    __shared__ double cs[9];
+    __shared__ double fp_sh;
+    int e = blockIdx.x;
+    int i = e % n1, j = e / n1;
+    int t = threadIdx.x;
+    double jac = (bp1[i + 1] - bp1[i]) * (bp2[j + 1] - bp2[j]);
+    if (t < 9) cs[t] = fc[(i + t % 3) + (j + t / 3) * nd1];
+    if (t == 0) {
+        double m = 0.0;
+        for (int k = 0; k < 9; k++) m += bS[(size_t)e * 9 + k];
+        fp_sh = m / jac;
+    }
+    __syncthreads();
+    int nqq = nq * nq;
+    if (t < nqq) {
+        int q1 = t % nq, q2 = t / nq;
+        double p1[3], p2[3];
+        for (int a = 0; a < 3; a++) {
+            p1[a] = Tq1[((size_t)i * 3 + a) * nq + q1];
+            p2[a] = Tq2[((size_t)j * 3 + a) * nq + q2];
+        }
+        double f = 0.0;
+        for (int b = 0; b < 3; b++)
+            for (int a = 0; a < 3; a++) f += cs[a + 3 * b] * (p1[a] * p2[b]);
+        double wq = qw[q1] * qw[q2];
+        double s = 0.0;
+        if (logsq) {
+            if (f * f > 1e-60) s = -(f * 0.5 * log(f * f) * wq * jac);
+        } else if (f > 1e-30) {
+            s = -(f * log(f) * wq * jac);
+        }
+        double d = f - fp_sh;
+        contrib[t * 3 + 0] = s;
+        contrib[t * 3 + 1] = f < 0.0 ? (-f) * wq * jac : 0.0;
+        contrib[t * 3 + 2] = d * d * wq * jac;
+    }
+    __syncthreads();
+    if (t < 3) {
+        double s = 0.0;
+        for (int q = 0; q < nqq; q++) s += contrib[q * 3 + t];
+        D[(size_t)e * 3 + t] = s;
+    }
+}
+
+// block partials of sum w v1, sum w v2, sum w |v|^2 over all markers
+// (compute_momentum / compute_energy, functions.jl:349-358)
+__global__ void __launch_bounds__(CO_RED_THREADS)
+k_marker_moments(const double *__restrict__ v, const double *__restrict__ w, int N,
+                 double *__restrict__ red) {
+    __shared__ double sh[32];
+    double p1 = 0.0, p2 = 0.0, e = 0.0;
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < N; a += gridDim.x * blockDim.x) {
+        double x1 = v[a], x2 = v[N + a], wa = w[a];
+        p1 += wa * x1;
+        p2 += wa * x2;
+        e += wa * (x1 * x1 + x2 * x2);
+    }
+    double s1 = co_block_sum(p1, sh);
+    double s2 = co_block_sum(p2, sh);
+    double s3 = co_block_sum(e, sh);
+    if (threadIdx.x == 0) {
+        red[blockIdx.x * 3 + 0] = s1;
+        red[blockIdx.x * 3 + 1] = s2;
+        red[blockIdx.x * 3 + 2] = s3;
+    }
+}
+
+// out = {S, E, P1, P2, ||f_s - f_p||_2, negative part}, fixed-order sums
+__global__ void __launch_bounds__(256)
+k_diag_final(const double *__restrict__ D, int n_el, const double *__restrict__ red, int nred,
+             double *__restrict__ out) {
+    __shared__ double sh[32];
+    double S = co_sum_partials(D, n_el, 3, 0, sh);
+    double neg = co_sum_partials(D, n_el, 3, 1, sh);
+    double sq = co_sum_partials(D, n_el, 3, 2, sh);
+    double p1 = co_sum_partials(red, nred, 3, 0, sh);
+    double p2 = co_sum_partials(red, nred, 3, 1, sh);
+    double e = co_sum_partials(red, nred, 3, 2, sh);
+    if (threadIdx.x == 0) {
+        out[0] = S;
+        out[1] = 0.5 * e;
+        out[2] = p1;
+        out[3] = p2;
+        out[4] = sqrt(sq);
+        out[5] = neg;
+    }
+}
+
 // S = sum_e Ep[e] in a fixed order (one block)
 __global__ void __launch_bounds__(256)
 k_sum_to(const double *__restrict__ Ep, int n, double *__restrict__ out) {
@@ -633,6 +734,24 @@ int co_entropy_parts_dev(co_ctx *c, const double *f) {
 int co_entropy_finalize_dev(co_ctx *c, double *S_dev) {
     k_sum_to<<<1, 256, 0, c->stream>>>(c->Ep, c->n_el, S_dev);
     c->launches++;
+    CO_CK(cudaGetLastError());
+    return CO_OK;
+}
+
+// post-step diagnostics of markers x (device) with weights in mb.w -> out6 (device)
+int co_diagnostics_impl(co_ctx *c, const double *x, int N, double *out6) {
+    int rc;
+    if ((rc = co_sort_markers(c, x, N))) return rc;
+    if ((rc = co_project_sorted(c, c->f))) return rc;
+    double *D = c->E;   // n_el x 9 scratch; the diagnostics use n_el x 3
+    k_diag_elem<<<c->n_el, 64, 0, c->stream>>>(c->f, c->n1, c->nd1, c->nq, c->Tq1, c->Tq2, c->qw,
+                                               c->bp1, c->bp2, (c->flags & CO_FLAG_LOGSQ) ? 1 : 0,
+                                               c->bS, D);
+    int g = co_cdiv(N > 0 ? N : 1, CO_RED_THREADS);
+    if (g > c->mb.red_cap) g = c->mb.red_cap;
+    k_marker_moments<<<g, CO_RED_THREADS, 0, c->stream>>>(x, c->mb.w, N, c->mb.red);
+    k_diag_final<<<1, 256, 0, c->stream>>>(D, c->n_el, c->mb.red, g, out6);
+    c->launches += 3;
     CO_CK(cudaGetLastError());
     return CO_OK;
 }

@@ -204,6 +204,15 @@ int co_predictor(co_ctx *ctx, const co_opts *opts, double *v1, const double *v,
 int co_predictor_dev(co_ctx *ctx, const co_opts *opts, double *v1,
                      const double *v, const double *w, int N, double dt);
 
+/* Post-step diagnostics of the time loop (main.jl:298-307): out6 (host) =
+ * {entropy S of the projection of v, energy 1/2 sum w |v|^2, momentum P1, P2,
+ * ||f_s - f_p||_2 with f_p the element-constant histogram density
+ * (compute_fs_minus_fp_l2, functions.jl:315-347), the negative-part L1 norm of
+ * f_s (compute_negative_part_l1, :300-313)}; Gauss grid of N_QUAD points per
+ * direction. co_diagnostics takes host arrays, co_diagnostics_dev device ones. */
+int co_diagnostics(co_ctx *ctx, const double *v, const double *w, int N, double *out6);
+int co_diagnostics_dev(co_ctx *ctx, const double *v, const double *w, int N, double *out6);
+
 /* Entropy of the projection of markers v (f_s(v) -> S), device pointers:
  * the S0 of the next step (main.jl:228, :298-300). */
 int co_entropy_of_markers_dev(co_ctx *ctx, const double *v, const double *w,

@@ -56,6 +56,7 @@ def _load():
     lib.om_entropy.restype = C.c_double
     lib.om_compute_G.argtypes = [C.c_void_p, _dp, C.c_int, _dp, _dp]
     lib.om_hessian_L.argtypes = [C.c_void_p, _dp, C.c_int, _dp, _dp]
+    lib.om_diagnostics.argtypes = [C.c_void_p, _dp, _dp, C.c_int, _dp]
     lib.om_loggrad.argtypes = [C.c_void_p, _dp, C.c_int, _dp, _dp]
     lib.om_eval_field.argtypes = [C.c_void_p, _dp, C.c_double, C.c_double]
     lib.om_eval_field.restype = C.c_double
@@ -200,6 +201,14 @@ class OracleMesh:
         v, L = _mk(v), np.ascontiguousarray(L, dtype=np.float64)
         out = np.zeros((v.shape[0], 2), order="F")
         self.lib.om_compute_G(self.h, _d(v), v.shape[0], _d(L), _d(out))
+        return out
+
+    def diagnostics(self, v, w) -> np.ndarray:
+        """(S, energy, P1, P2, ||f_s - f_p||_2, negative-part L1) of markers v."""
+        v = _mk(v)
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        out = np.zeros(6)
+        self.lib.om_diagnostics(self.h, _d(v), _d(w), v.shape[0], _d(out))
         return out
 
     def hessian_L(self, v, L) -> np.ndarray:

@@ -383,6 +383,51 @@ double om_entropy(const om_mesh *m, const double *f) {
     return S;
 }
 
+/* Post-step diagnostics of the time loop (main.jl:298-307): out6 = entropy S of
+ * the projection of v, energy 1/2 sum w |v|^2 (compute_energy, functions.jl:355-358),
+ * momentum sum w v (compute_momentum, :349-353), ||f_s - f_p||_2 with f_p the
+ * element-constant histogram density (compute_fs_minus_fp_l2, :315-347) and the
+ * negative-part L1 norm of f_s (compute_negative_part_l1, :300-313), both on the
+ * N_QUAD Gauss grid. Element masses are summed over the markers located in
+ * each element, as the reference does. */
+void om_diagnostics(const om_mesh *m, const double *v, const double *w, int N, double *out6) {
+    double *f = malloc(sizeof(double) * m->n_dofs);
+    double *emass = calloc((size_t)m->n1 * m->n2, sizeof(double));
+    om_l2_project(m, v, w, N, f);
+    double E = 0.0, P1 = 0.0, P2 = 0.0;
+    for (int a = 0; a < N; a++) {
+        P1 += w[a] * v[a];
+        P2 += w[a] * v[N + a];
+        E += w[a] * (v[a] * v[a] + v[N + a] * v[N + a]);
+        loc_t L;
+        if (locate(m, v[a], v[N + a], &L)) emass[L.i + L.j * m->n1] += w[a];
+    }
+    double sumsq = 0.0, neg = 0.0;
+    for (int ej = 0; ej < m->n2; ej++)
+        for (int ei = 0; ei < m->n1; ei++) {
+            double jac = (m->bp1[ei + 1] - m->bp1[ei]) * (m->bp2[ej + 1] - m->bp2[ej]);
+            double fp = emass[ei + ej * m->n1] / jac;
+            for (int q2 = 0; q2 < m->nq; q2++)
+                for (int q1 = 0; q1 < m->nq; q1++) {
+                    double phi[9];
+                    int gids[9];
+                    double fv = field_at_qp(m, f, ei, ej, q1, q2, phi, gids);
+                    double wq = m->qw[q1] * m->qw[q2];
+                    if (fv < 0.0) neg += (-fv) * wq * jac;
+                    double d = fv - fp;
+                    sumsq += d * d * wq * jac;
+                }
+        }
+    out6[0] = om_entropy(m, f);
+    out6[1] = 0.5 * E;
+    out6[2] = P1;
+    out6[3] = P2;
+    out6[4] = sqrt(sumsq);
+    out6[5] = neg;
+    free(f);
+    free(emass);
+}
+
 /* compute_r! (functions.jl:158-179) */
 void om_compute_r(const om_mesh *m, const double *f, double *r) {
     memset(r, 0, sizeof(double) * m->n_dofs);

@@ -109,6 +109,9 @@ typedef struct {
 void om_picard_map(const om_mesh *m, const om_opts *o, double *v_out,
                    const double *v_in, const double *v0, const double *w,
                    int N, double S0, double dt);
+/* Post-step diagnostics (main.jl:298-307): out6 = S, energy, momentum (2),
+ * ||f_s - f_p||_2 (histogram density), integral of max(-f_s, 0). */
+void om_diagnostics(const om_mesh *m, const double *v, const double *w, int N, double *out6);
 /* step_anderson!  (solver.jl:300-423). v1: initial guess in, solution out.
  * out4 = iterations, residual, n_restarts, initial residual. */
 void om_step_anderson(const om_mesh *m, const om_opts *o, double *v1,

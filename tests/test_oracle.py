@@ -235,6 +235,32 @@ def test_oracle_step_conserves(oracle_mod, model):
 
 # ---------------------------------------------------- golden vectors
 
+def test_diagnostics_known_answers(mesh16, oracle_mod):
+    """om_diagnostics: momentum and energy are the reference's known answers
+    (test/integration/main_helpers.jl:13-19), the entropy equals the projection's
+    S, and for markers spread uniformly over a cell-aligned block the histogram
+    error is small against the density itself while a concentrated clump shows
+    a Gibbs negative lobe."""
+    om, bp = mesh16
+    v = np.asfortranarray([[1.0, 2.0], [-3.0, 0.5]])
+    w = np.array([0.25, 0.75])
+    d = om.diagnostics(v, w)
+    assert np.isclose(d[2], 0.25 * 1.0 + 0.75 * -3.0) and np.isclose(d[3], 0.25 * 2.0 + 0.75 * 0.5)
+    assert np.isclose(d[1], 0.5 * (0.25 * (1.0 + 4.0) + 0.75 * (9.0 + 0.25)))
+    rng = np.random.default_rng(8)
+    vg, wg = gaussian_markers(4096, 1.0, 0.5, seed=8)
+    dg = om.diagnostics(vg, wg)
+    assert np.isclose(dg[0], om.entropy(om.l2_project(vg, wg)), rtol=1e-14)
+    # uniform markers on [-3,3]^2 (cell-aligned): f_s ~ f_p ~ 1/36 in the block
+    vu = np.asfortranarray(rng.uniform(-3.0, 3.0, size=(200000, 2)))
+    du = om.diagnostics(vu, np.full(200000, 1 / 200000))
+    assert du[4] < 0.2 * np.sqrt(1 / 36.0)
+    # a tight clump: the projection rings and has a negative part
+    vc = np.asfortranarray(0.01 * rng.standard_normal((2000, 2)))
+    dc = om.diagnostics(vc, np.full(2000, 1 / 2000))
+    assert dc[5] > 0.0
+
+
 def test_hessian_matches_gradient_differences(mesh16, oracle_mod):
     """The Hessian gather of the block preconditioner equals central differences
     of the gradient gather compute_G on the same field (away from cell edges)."""

@@ -336,6 +336,29 @@ def test_step_defect_metric_freeze_c1(built_lib, oracle_mod, collops_mod):
     ws.close()
 
 
+@pytest.mark.parametrize("logsq", [False, True])
+def test_diagnostics_c2(built_lib, oracle_mod, collops_mod, logsq):
+    """Post-step diagnostics (entropy, energy, momentum, ||f_s - f_p||_2,
+    negative-part L1) against the oracle, bimodal markers on [-8,8]^2 with a
+    32x32 mesh (the tails give a nonzero negative part)."""
+    bp = uniform_bp(-8.0, 8.0, 32)
+    rng = np.random.default_rng(21)
+    N = 16384
+    v = np.zeros((N, 2), order="F")
+    v[:, 0] = np.where(np.arange(N) < N // 2, -2.0, 2.0) + np.sqrt(0.5) * rng.standard_normal(N)
+    v[:, 1] = np.sqrt(0.5) * rng.standard_normal(N)
+    w = np.full(N, 1.0 / N)
+    om = oracle_mod.OracleMesh(bp, bp, 6, use_logsq=logsq)
+    ref = om.diagnostics(v, w)
+    ws = collops_mod.build_workspace(collops_mod.SimParameters(bp1=bp, bp2=bp, use_logsq=logsq))
+    d = collops_mod.diagnostics(ws, v, w)
+    ws.close()
+    got = np.array([d["entropy"], d["energy"], *d["momentum"], d["fs_minus_fp_l2"],
+                    d["negative_part_l1"]])
+    assert ref[5] > 0.0
+    np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-15)
+
+
 def test_step_defect_c1(built_lib, oracle_mod, collops_mod):
     """step_defect! against the oracle's (same algorithm, FP64 metric): the same
     fixed point. The implicit step can have several fixed points (two solvers
