@@ -665,10 +665,10 @@ def main(argv=None):
     ap.add_argument("--dc-eta", type=float, default=0.05)
     ap.add_argument("--dc-max-inner", type=int, default=60)
     ap.add_argument("--dc-stag-window", type=int, default=5)
-    ap.add_argument("--dc-fp32-stall", type=float, default=0.5,
+    ap.add_argument("--dc-fp32-stall", type=float, default=0.9,
                     help="the mixed forms leave FP32 outer maps once a map cuts the residual "
                          "by less than this factor")
-    ap.add_argument("--dc-outer-m", type=int, default=0,
+    ap.add_argument("--dc-outer-m", type=int, default=5,
                     help="Anderson depth over the defect correction's outer iterates")
     ap.add_argument("--dc-precond", type=int, default=0, choices=[0, 1, 2],
                     help="block-Newton preconditioner of the inner iteration")
