@@ -7,9 +7,9 @@ the start of a step to the normalised correction of the explicit predictor,
 the form of warm start the reference planned ("Euler + dt^2 * delta" MLP
 correction, Parameters.jl:108-112; its warmstart_nn.jl is not in the tree).
 
-The fixed-point map stays the judge: `propose` returns the learned iterate only
-when its first Picard residual (one map at the solver's precision) is smaller
-than that of the plain predictor; otherwise the predictor is used.
+The fixed-point map decides: `propose` returns the learned iterate only when
+its first Picard residual (one FP32 map in the mixed forms) is smaller than
+that of the plain predictor; otherwise the predictor is used.
 
 Training data comes from the solver itself: `generate_pairs` runs time steps
 and records (features at the step start, delta of the converged step).

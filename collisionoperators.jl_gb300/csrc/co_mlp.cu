@@ -15,8 +15,8 @@
 // features at the start of a step (velocity, entropy gradient, predictor
 // velocity, log-density and its gradient) to the normalised correction
 // (v_converged - v_Euler)/dt^2, in the spirit of the reference's planned
-// "Euler + dt^2 * delta" correction (Parameters.jl:108-112). The solver stays
-// the judge: the caller keeps the plain predictor whenever the learned
+// "Euler + dt^2 * delta" correction (Parameters.jl:108-112). The solver keeps
+// the last word: the caller keeps the plain predictor whenever the learned
 // proposal's first residual is larger.
 #include <cuda_bf16.h>
 #include <math.h>

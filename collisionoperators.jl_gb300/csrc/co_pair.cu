@@ -20,7 +20,7 @@
 // higher-order step in place of two quadratic ones). The |d|^2 < 1e-24 guard
 // (functions.jl:224) is an integer compare on the bit pattern.
 //
-// Mixed form (BASELINE precision form): the pair arithmetic runs in FP32 on
+// Mixed form (the precision form of the solver): the pair arithmetic runs in FP32 on
 // FP64-centred differences -- each coordinate is split into an FP32 head and
 // tail (x = xh + xl), so d = (xh_g - xh_a) + (xl_g - xl_a) is accurate to an
 // FP32 rounding of d itself even for close pairs -- and the per-tile FP32
