@@ -255,7 +255,8 @@ def run_gpu(args, cfg):
         return S.value
 
     dopt = co.CoDefectOpts(args.dc_eta, args.dc_max_inner, args.dc_stag_window, args.dc_fp32_stall, 0,
-                           args.dc_outer_m, args.dc_precond, args.dc_metric_freeze)
+                           args.dc_outer_m, args.dc_precond, args.dc_metric_freeze,
+                           args.dc_fp32_window)
 
     warm = None
     if args.warmstart == "learned":
@@ -668,6 +669,9 @@ def main(argv=None):
     ap.add_argument("--dc-fp32-stall", type=float, default=0.9,
                     help="the mixed forms leave FP32 outer maps once a map cuts the residual "
                          "by less than this factor")
+    ap.add_argument("--dc-fp32-window", type=int, default=0,
+                    help="leave FP32 outer maps after this many maps without a new best "
+                         "residual (0: after the first map below the stall cut)")
     ap.add_argument("--dc-outer-m", type=int, default=5,
                     help="Anderson depth over the defect correction's outer iterates")
     ap.add_argument("--dc-precond", type=int, default=0, choices=[0, 1, 2],

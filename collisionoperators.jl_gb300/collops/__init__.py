@@ -77,7 +77,7 @@ class CoDefectOpts(C.Structure):
     """co_defect_opts of include/collops.h."""
     _fields_ = [("eta", C.c_double), ("max_inner", C.c_int), ("stag_window", C.c_int),
                 ("fp32_stall", C.c_double), ("metric64", C.c_int), ("outer_m", C.c_int),
-                ("precond", C.c_int), ("metric_freeze", C.c_double)]
+                ("precond", C.c_int), ("metric_freeze", C.c_double), ("fp32_window", C.c_int)]
 
 
 class CoBatchInstance(C.Structure):
@@ -497,7 +497,8 @@ def step_defect(ws: Workspace, v1, v0, w_parts, S0: float, dt: float, *, m: int 
                 damping: float = 0.7, eta: float = 0.05, max_inner: int = 60,
                 stag_window: int = 5, stag_rel_tol: float = 0.1, use_gonzalez: bool = True,
                 precision: str = "fp64", metric64: bool = True, fp32_stall: float = 0.5,
-                outer_m: int = 0, precond: int = 0, metric_freeze: float = 0.0):
+                outer_m: int = 0, precond: int = 0, metric_freeze: float = 0.0,
+                fp32_window: int = 0):
     """step_defect! (solver.jl:569-634) on the device; v1 (guess) is overwritten with
     the solution. Returns (outer_iterations, residual, inner_iterations, initial_residual).
     outer_m > 0 mixes the outer iterates by Anderson and precond = 1 preconditions the
@@ -510,7 +511,7 @@ def step_defect(ws: Workspace, v1, v0, w_parts, S0: float, dt: float, *, m: int 
                   stag_rel_tol=stag_rel_tol, use_gonzalez=int(use_gonzalez),
                   precision=_PREC[precision])
     d = CoDefectOpts(eta, max_inner, stag_window, fp32_stall, int(metric64), int(outer_m),
-                     int(precond), float(metric_freeze))
+                     int(precond), float(metric_freeze), int(fp32_window))
     it, inner = C.c_int(), C.c_int()
     res, r0 = C.c_double(), C.c_double()
     _check(ws.lib.co_step_defect(ws.h, C.byref(o), C.byref(d), _p(v1), _p(v0),

@@ -36,6 +36,8 @@ struct co_solver_state {
     int improved;        // nrm_r < nrm_best at the current k
     int error;           // device-detected error (non-finite residual, timeout)
     double nrm_r0, nrm_r, nrm_v, nrm_best, nrm_best_window, damp, res_out;
+    double best32;       // defect correction: best FP32-stage outer residual
+    int kbest32;         // and the outer map that reached it
     double ATA[CO_MAX_M * CO_MAX_M];
     double gamma[CO_MAX_M];
     double lambda;       // Gonzalez correction of the current map

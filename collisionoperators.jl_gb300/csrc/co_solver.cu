@@ -290,6 +290,8 @@ __global__ void k_state_reset(co_solver_state *st) {
         st->nrm_best = INFINITY;
         st->nrm_best_window = INFINITY;
         st->res_out = 0.0;
+        st->best32 = INFINITY;
+        st->kbest32 = 0;
     }
 }
 
@@ -885,7 +887,7 @@ __global__ void k_precond(int N, const double *__restrict__ A, const double *__r
 
 struct co_defect_dev {
     double tol, abs_floor, eta, stag_rel_tol, fp32_stall;
-    int stag_window;
+    int stag_window, fp32_window;
 };
 
 // outer decisions (solver.jl:603-626). stage: 1 = FP32 outer map, 0 = FP64.
@@ -913,12 +915,25 @@ k_ctrl_outer(const double *__restrict__ red, int nred, co_solver_state *st, co_d
     }
     st->improved = 0;
     if (stage == 1) {
-        // FP32 outer maps: stop them once the residual no longer halves
-        // (the FP32 noise floor); the FP64 stage then takes over
+        // FP32 outer maps: stop them at the FP32 noise floor, where the FP64
+        // stage takes over. fp32_window = 0: as soon as a map cuts the residual
+        // by less than fp32_stall; fp32_window = W > 0: once W maps in a row
+        // brought no new best cut by fp32_stall (robust to the non-monotone
+        // residuals of the outer Anderson mixing)
         double prev = st->nrm_r;
         st->nrm_r = nrm;
         if (k == 1) st->nrm_r0 = nrm;
-        if ((k > 1 && nrm > o.fp32_stall * prev) || nrm < fmax(o.tol * (nv + 1e-30), o.abs_floor))
+        bool stall;
+        if (o.fp32_window > 0) {
+            if (nrm < o.fp32_stall * st->best32) {
+                st->best32 = nrm;
+                st->kbest32 = k;
+            }
+            stall = k - st->kbest32 >= o.fp32_window;
+        } else {
+            stall = k > 1 && nrm > o.fp32_stall * prev;
+        }
+        if (stall || nrm < fmax(o.tol * (nv + 1e-30), o.abs_floor))
             st->path = 0;
         else
             st->path = 1;
@@ -1098,6 +1113,8 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
     d.stag_rel_tol = o->stag_rel_tol;
     d.stag_window = dopt->stag_window;
     d.fp32_stall = dopt->fp32_stall > 0 ? dopt->fp32_stall : 0.5;
+    d.fp32_window = dopt->fp32_window;
+    if (d.fp32_window < 0) return CO_ERR_ARG;
     co_dev_opts di = dev_opts(o, 0.0);
     int stage = o->precision != CO_PREC_FP64 ? 1 : 0;
     const int ds = o->precision == CO_PREC_MIXED_DS;  // FP64 stage in double-single

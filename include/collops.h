@@ -184,6 +184,10 @@ typedef struct {
                        ||r_1|| (A only shapes the inner model, so near the
                        fixed point the last A serves); 0 rebuilds it at every
                        outer map, as the reference does                       */
+    int fp32_window; /* mixed forms: 0 leaves the FP32 outer maps as soon as one
+                       map cuts the residual by less than fp32_stall; W > 0
+                       once W maps in a row brought no new best residual cut
+                       by fp32_stall                                          */
 } co_defect_opts;
 
 /* step_defect! (solver.jl:569-634): defect correction around a frozen
