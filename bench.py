@@ -663,8 +663,8 @@ def main(argv=None):
     ap.add_argument("--warmstart", choices=["learned", "euler"], default="learned")
     ap.add_argument("--warmstart-file", default=os.path.join(
         PKG, "collops", "warmstart_c3.npz"))
-    ap.add_argument("--dc-eta", type=float, default=0.05)
-    ap.add_argument("--dc-max-inner", type=int, default=60)
+    ap.add_argument("--dc-eta", type=float, default=0.02)
+    ap.add_argument("--dc-max-inner", type=int, default=100)
     ap.add_argument("--dc-stag-window", type=int, default=5)
     ap.add_argument("--dc-fp32-stall", type=float, default=0.9,
                     help="the mixed forms leave FP32 outer maps once a map cuts the residual "

@@ -69,10 +69,10 @@ def run(weights: str, steps: int = 3, solver: str = "anderson", form: str = "mix
     x = torch.from_numpy(np.ascontiguousarray(v_np.T)).to(dev)
     w = torch.from_numpy(w_np).to(dev)
     v1 = torch.empty_like(x)
-    # the benchmark's defect-correction settings: eta 0.05, 60 inner maps, stagnation
+    # the benchmark's defect-correction settings: eta 0.02, 100 inner maps, stagnation
     # window 5, FP32 stage left below a 0.9 cut, outer Anderson depth 5, no inner
     # preconditioner, FP32 metric frozen after a 100x residual drop
-    dopt = co.CoDefectOpts(0.05, 60, 5, 0.9, 0, 5, 0, 1e-2)
+    dopt = co.CoDefectOpts(0.02, 100, 5, 0.9, 0, 5, 0, 1e-2, 0)
 
     def entropy(xx):
         S = C.c_double()
