@@ -388,7 +388,6 @@ k_anderson_cols(int n2, co_solver_state *st, const double *__restrict__ r,
                 double *__restrict__ rp, const double *__restrict__ Gv, double *__restrict__ Gp,
                 double *__restrict__ dF, double *__restrict__ dG, size_t ldF,
                 double *__restrict__ red) {
-    __shared__ double sh[32];
     if (st->done || st->path != 1) return;
     const int slot = st->slot - 1, hist = st->history;
     double pa[CO_MAX_M], pb[CO_MAX_M];
@@ -407,31 +406,49 @@ k_anderson_cols(int n2, co_solver_state *st, const double *__restrict__ r,
             pb[j] += fj * ri;
         }
     }
+    // all 2*hist block sums at once: shuffle trees per warp, then warp partials
+    // summed in warp order by one thread per value (fixed order, one barrier)
+    __shared__ double wsum[CO_RED_THREADS / 32][2 * CO_MAX_M];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int j = 0; j < hist; j++) {
-        double a = co_block_sum(pa[j], sh);
-        double b = co_block_sum(pb[j], sh);
-        if (threadIdx.x == 0) {
-            red[(size_t)blockIdx.x * 2 * CO_MAX_M + j] = a;
-            red[(size_t)blockIdx.x * 2 * CO_MAX_M + CO_MAX_M + j] = b;
+        double a = pa[j], b = pb[j];
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_down_sync(0xffffffffu, a, o);
+            b += __shfl_down_sync(0xffffffffu, b, o);
         }
+        if (lane == 0) {
+            wsum[warp][j] = a;
+            wsum[warp][CO_MAX_M + j] = b;
+        }
+    }
+    __syncthreads();
+    const int t = threadIdx.x;
+    if (t < 2 * CO_MAX_M && (t % CO_MAX_M) < hist) {
+        double s = 0.0;
+        for (int w = 0; w < nw; w++) s += wsum[w][t];
+        red[(size_t)blockIdx.x * 2 * CO_MAX_M + t] = s;
     }
 }
 
 // normal equations with Tikhonov shift, gamma = ATA \ ATr (solver.jl:396-409)
 __global__ void __launch_bounds__(256)
 k_anderson_solve(const double *__restrict__ red, int nred, co_solver_state *st, co_dev_opts o) {
-    __shared__ double sh[32];
     __shared__ double dots[2 * CO_MAX_M];
     if (st->done || st->path != 1) return;
     const int slot = st->slot - 1, h = st->history;
-    for (int j = 0; j < h; j++) {
-        double a = co_sum_partials(red, nred, 2 * CO_MAX_M, j, sh);
-        double b = co_sum_partials(red, nred, 2 * CO_MAX_M, CO_MAX_M + j, sh);
-        if (threadIdx.x == 0) {
-            dots[j] = a;
-            dots[CO_MAX_M + j] = b;
+    // the 2h sums over the nred block partials: one warp per value, lanes stride
+    // the partials in order, then a shuffle tree (fixed order)
+    {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        for (int c = warp; c < 2 * h; c += nw) {
+            const int col = c < h ? c : CO_MAX_M + (c - h);
+            double s = 0.0;
+            for (int i = lane; i < nred; i += 32) s += red[(size_t)i * 2 * CO_MAX_M + col];
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+            if (lane == 0) dots[col] = s;
         }
     }
+    __syncthreads();
     if (threadIdx.x != 0) return;
     for (int j = 0; j < h; j++) {
         st->ATA[slot * CO_MAX_M + j] = dots[j];
