@@ -129,6 +129,15 @@ class WarmStart:
         self.ts = np.ones(self.mlp.n_out)
         self._xm_dev = self._xs_dev = None   # device copies of xm, xs
 
+    def validation_loss(self, X: np.ndarray, T: np.ndarray, device: int = 0) -> float:
+        """Mean squared error of the normalised prediction on (X, T) (co_mlp_gradients
+        computes the loss; the gradient is discarded)."""
+        import torch
+        Xn = torch.from_numpy(((X - self.xm) / self.xs).astype(np.float32)).cuda(device)
+        Tn = torch.from_numpy(((T - self.tm) / self.ts).astype(np.float32)).cuda(device)
+        _g, loss = self.mlp.gradients(Xn.contiguous(), Tn.contiguous())
+        return float(loss)
+
     def fit(self, X: np.ndarray, T: np.ndarray, epochs: int = 20, batch: int = 8192,
             lr: float = 2e-3, seed: int = 0, device: int = 0):
         """Train on the GPU with the library's kernels; returns the loss history."""

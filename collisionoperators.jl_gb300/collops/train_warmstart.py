@@ -98,13 +98,18 @@ def main(argv=None):
     t0 = time.time()
     X, T = collect(a.pairs)
     t1 = time.time()
+    # hold out every 20th pair for a validation loss
+    rng = np.random.default_rng(5)
+    held = rng.random(X.shape[0]) < 0.05
     ws = learned.WarmStart()
-    hist = ws.fit(X, T, epochs=a.epochs, batch=a.batch, lr=a.lr)
+    hist = ws.fit(X[~held], T[~held], epochs=a.epochs, batch=a.batch, lr=a.lr)
+    val = ws.validation_loss(X[held], T[held])
     t2 = time.time()
     ws.save(a.out)
-    print(json.dumps({"pairs": int(X.shape[0]), "collect_s": round(t1 - t0, 1),
-                      "train_s": round(t2 - t1, 1), "loss_first": hist[0],
-                      "loss_last": hist[-1], "epochs": a.epochs}))
+    print(json.dumps({"pairs": int(X.shape[0]), "held_out": int(held.sum()),
+                      "collect_s": round(t1 - t0, 1), "train_s": round(t2 - t1, 1),
+                      "loss_first": hist[0], "loss_last": hist[-1], "val_loss": val,
+                      "epochs": a.epochs}))
 
 
 if __name__ == "__main__":
