@@ -532,6 +532,22 @@ def diagnostics(ws: Workspace, v_parts, w_parts) -> dict:
                 negative_part_l1=out[5])
 
 
+# columns of the reference's per-step conservation CSV (io.jl CONS_COLS)
+CONS_COLS = ("step", "time", "entropy", "energy", "momentum_1", "momentum_2", "iter",
+             "residual", "fp_minus_fs", "neg_part", "r0", "dt")
+
+
+def conservation_row(step: int, time: float, diag: dict, iters: int, residual: float,
+                     r0: float, dt: float) -> str:
+    """One row of the conservation CSV the reference's time loop appends after
+    each step (main.jl:309-317; columns io.jl CONS_COLS), from `diagnostics()`
+    and the step's solver record, so the reference's dashboards read it."""
+    vals = (step, time, diag["entropy"], diag["energy"], diag["momentum"][0],
+            diag["momentum"][1], iters, residual, diag["fs_minus_fp_l2"],
+            diag["negative_part_l1"], r0, dt)
+    return ",".join(repr(float(x)) if isinstance(x, float) else str(x) for x in vals)
+
+
 def predictor(ws: Workspace, v1, v_parts, w_parts, dt: float, precision: str = "fp64") -> None:
     """Explicit predictor of the time loop (main.jl:233-245): v1 = v + dt vdot(v)."""
     v = _markers(v_parts, name="v_parts")

@@ -107,3 +107,17 @@ def test_output_layout_checked(collops_mod):
     with pytest.raises(ValueError):
         collops_mod._out(np.zeros((4, 2)), (4, 2), "dot_v")   # C order
     collops_mod._out(np.zeros((4, 2), order="F"), (4, 2), "dot_v")
+
+
+def test_conservation_row_layout(collops_mod):
+    """conservation_row writes the reference's CONS_COLS in order (io.jl)."""
+    assert collops_mod.CONS_COLS == ("step", "time", "entropy", "energy", "momentum_1",
+                                     "momentum_2", "iter", "residual", "fp_minus_fs",
+                                     "neg_part", "r0", "dt")
+    d = dict(entropy=2.5, energy=0.625, momentum=(1e-17, -2e-17), fs_minus_fp_l2=0.1,
+             negative_part_l1=0.002)
+    row = collops_mod.conservation_row(3, 0.06, d, 18, 3e-10, 6.5, 0.02)
+    fields = row.split(",")
+    assert len(fields) == len(collops_mod.CONS_COLS)
+    assert fields[0] == "3" and fields[6] == "18"
+    assert float(fields[2]) == 2.5 and float(fields[5]) == -2e-17 and float(fields[11]) == 0.02
