@@ -485,7 +485,10 @@ def run_gpu(args, cfg):
         flops = 23.0 * pairs / launches            # 23 algorithmic flops per ordered pair
         achieved = flops / (avg_ms * 1e-3) / 1e12
         pk = peak / 1e12
-        return {"bound": kind, "achieved": round(achieved, 3), "peak": round(pk, 3),
+        return {"bound": kind,
+                "bound_note": "SIMT pipe bound (FP32 FMA or FP64): an N-body pair sum, no "
+                              "tensor-core contraction; inputs are L2-resident, so not HBM",
+                "achieved": round(achieved, 3), "peak": round(pk, 3),
                 "unit": "TFLOP/s", "frac": round(achieved / pk, 4), "traffic": None,
                 "kernel": "k_pair32" if kind == "fp32" else "k_pair64<false>",
                 "avg_launch_ms": round(avg_ms, 3), "launches": launches,
