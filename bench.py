@@ -514,6 +514,12 @@ def run_gpu(args, cfg):
     traffic = load_traffic()
     if dominant and traffic.get(dominant["kernel"]) is not None:
         dominant["traffic"] = traffic[dominant["kernel"]]
+    for rr in (r32, r64, rds):
+        if rr:
+            for key in ("ncu_issue_active", "ncu_fma_pipe", "ncu_fp64_pipe"):
+                val = load_profile_lines(key).get(rr["kernel"])
+                if val is not None:
+                    rr[key] = val
 
     maps_fp64 = None
     maps_src = None
@@ -568,24 +574,28 @@ def run_gpu(args, cfg):
         dist.destroy_process_group()
 
 
-def load_traffic():
-    """DRAM bytes per launch from the committed ncu summaries (profiles/*.md lines
-    'traffic_bytes_per_launch <kernel>: <bytes>')."""
+def load_profile_lines(key: str = "traffic_bytes_per_launch"):
+    """Per-kernel figures from the committed ncu summaries: profiles/*.md lines
+    '<key> <kernel>: <value>' (DRAM bytes per launch, pipe fractions)."""
     out = {}
     d = os.path.join(ROOT, "profiles")
     if not os.path.isdir(d):
         return out
-    for fn in os.listdir(d):
+    for fn in sorted(os.listdir(d)):
         if not fn.endswith(".md"):
             continue
         for line in open(os.path.join(d, fn)):
-            if line.startswith("traffic_bytes_per_launch "):
-                k, val = line[len("traffic_bytes_per_launch "):].split(":")
+            if line.startswith(key + " "):
+                k, val = line[len(key) + 1:].split(":")
                 try:
                     out[k.strip()] = float(val)
                 except ValueError:
                     pass
     return out
+
+
+def load_traffic():
+    return load_profile_lines("traffic_bytes_per_launch")
 
 
 def run_reference(args, cfg):
