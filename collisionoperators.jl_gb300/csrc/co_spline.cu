@@ -251,10 +251,12 @@ __global__ void k_mass1(const double *__restrict__ Minv1, const double *__restri
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nd1 * nd2) return;
     int i1 = t % nd1, i2 = t / nd1;
-    const double *row = Minv1 + (size_t)i1 * nd1;
+    // Minv1 is exactly symmetric (symmetrised at set-up), so its row i1 is read
+    // as column i1: consecutive threads read consecutive addresses (the same
+    // products in the same order as the row form)
     const double *col = b + (size_t)i2 * nd1;
     double s = 0.0;
-    for (int k = 0; k < nd1; k++) s = fma(row[k], col[k], s);
+    for (int k = 0; k < nd1; k++) s = fma(Minv1[(size_t)k * nd1 + i1], col[k], s);
     y[t] = s;
 }
 
