@@ -503,8 +503,10 @@ def run_gpu(args, cfg):
         rds["kernel"] = "k_pair_ds_sym"
         rds["fp64_equivalent_frac"] = round(rds["achieved"] / (peak64.value / 1e12), 3)
         rds["note"] = ("double-single (FP32 head+tail) arithmetic: 23 FP64-equivalent flops per "
-                       "pair, executed as ~130 FP32 instructions; frac is against the FP32 peak, "
-                       "fp64_equivalent_frac against the measured FP64 peak")
+                       "ordered pair, executed as ~210 FP32-pipe instructions per unordered pair "
+                       "(ncu); frac is against the FP32 peak by the 23-flop count, "
+                       "fp64_equivalent_frac against the measured FP64 peak, ncu_issue_active the "
+                       "fraction of issue slots the kernel keeps busy")
     if r32:
         r32["kernel"] = "k_pair32_sym"
     if r64:
