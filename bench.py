@@ -692,7 +692,7 @@ def main(argv=None):
     ap.add_argument("--dc-precond", type=int, default=0, choices=[0, 1, 2],
                     help="block-Newton preconditioner of the inner iteration")
     ap.add_argument("--no-accuracy", dest="accuracy", action="store_false")
-    ap.add_argument("--dc-metric-freeze", type=float, default=1e-2,
+    ap.add_argument("--dc-metric-freeze", type=float, default=1e-3,
                     help="stop rebuilding the FP32 frozen metric once ||r|| < this x ||r_1||")
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=2)

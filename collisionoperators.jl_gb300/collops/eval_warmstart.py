@@ -71,8 +71,8 @@ def run(weights: str, steps: int = 3, solver: str = "anderson", form: str = "mix
     v1 = torch.empty_like(x)
     # the benchmark's defect-correction settings: eta 0.02, 100 inner maps, stagnation
     # window 5, FP32 stage left below a 0.9 cut, outer Anderson depth 5, no inner
-    # preconditioner, FP32 metric frozen after a 100x residual drop
-    dopt = co.CoDefectOpts(0.02, 100, 5, 0.9, 0, 5, 0, 1e-2, 0)
+    # preconditioner, FP32 metric frozen after a 1000x residual drop
+    dopt = co.CoDefectOpts(0.02, 100, 5, 0.9, 0, 5, 0, 1e-3, 0)
 
     def entropy(xx):
         S = C.c_double()
