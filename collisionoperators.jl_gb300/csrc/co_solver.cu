@@ -14,6 +14,15 @@
 // The Anderson control (solver.jl:334-417) runs in one-block kernels that own
 // the device state; the host only launches the fixed kernel sequence of an
 // iteration and reads the `done` word.
+//
+// Also here:
+//   - step_defect! (solver.jl:569-634) with the staged precision of the mixed
+//     forms, and the optional outer Anderson mixing, inner preconditioner and
+//     metric freeze;
+//   - the explicit predictor (main.jl:233-245);
+//   - the batch engine (many ensembles, one persistent pair launch per
+//     iteration, graph replay over the live instances);
+//   - the warm-start entry points (features, proposal, first residual).
 #include <math.h>
 
 #include "co_internal.cuh"
