@@ -695,7 +695,7 @@ def main(argv=None):
     ap.add_argument("--dc-metric-freeze", type=float, default=1e-3,
                     help="stop rebuilding the FP32 frozen metric once ||r|| < this x ||r_1||")
     ap.add_argument("--plain-steps", type=int, default=1)
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--mixed-floor", type=float, default=0.0)
     ap.add_argument("--cpu-rows", type=int, default=32768)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
