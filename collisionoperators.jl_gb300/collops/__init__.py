@@ -80,6 +80,22 @@ class CoDefectOpts(C.Structure):
                 ("precond", C.c_int), ("metric_freeze", C.c_double), ("fp32_window", C.c_int)]
 
 
+class CoStepInfo(C.Structure):
+    """co_step_info of include/collops.h."""
+    _fields_ = [("outer", C.c_int), ("inner", C.c_int), ("res", C.c_double),
+                ("r0", C.c_double), ("converged", C.c_int), ("exit", C.c_int),
+                ("start", C.c_int), ("attempts", C.c_int), ("r_start", C.c_double * 3),
+                ("S_new", C.c_double)]
+
+    START_NAMES = ("predictor", "learned", "previous")
+
+    def as_dict(self) -> dict:
+        return dict(outer=self.outer, inner=self.inner, res=self.res, r0=self.r0,
+                    converged=bool(self.converged), exit=self.exit,
+                    start=self.START_NAMES[self.start], attempts=self.attempts,
+                    r_start=list(self.r_start), S_new=self.S_new)
+
+
 class CoBatchInstance(C.Structure):
     """co_batch_instance of include/collops.h."""
     _fields_ = [("bp1", C.POINTER(C.c_double)), ("nb1", C.c_int), ("bp2", C.POINTER(C.c_double)),
@@ -120,6 +136,7 @@ _SIGNATURES = {
                                    C.c_void_p, C.c_int, C.c_double]),
     "co_entropy_of_markers_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, _dp]),
     "co_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_ulonglong)]),
+    "co_ctx_set_wait_limit": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "co_ctx_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "co_profile": (C.c_int, [C.c_void_p, C.c_int]),
     "co_profile_read": (C.c_int, [C.c_void_p, C.POINTER(CoProfile)]),
@@ -153,6 +170,13 @@ _SIGNATURES = {
                                          C.c_double, _dp, _dp, C.c_void_p]),
     "co_picard_residual_dev": (C.c_int, [C.c_void_p, C.POINTER(CoOpts), C.c_void_p, C.c_void_p,
                                          C.c_void_p, C.c_int, C.c_double, C.c_double, _dp]),
+    "co_mlp_set_normalization": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp]),
+    "co_step_learned": (C.c_int, [C.c_void_p, C.POINTER(CoOpts), C.POINTER(CoDefectOpts),
+                                  C.c_void_p, C.c_int, _dp, _dp, _dp, C.c_int, C.c_double,
+                                  C.c_double, C.POINTER(CoStepInfo)]),
+    "co_step_learned_dev": (C.c_int, [C.c_void_p, C.POINTER(CoOpts), C.POINTER(CoDefectOpts),
+                                      C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_int, C.c_double, C.c_double, C.POINTER(CoStepInfo)]),
     "co_collision_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                        C.c_double, C.c_double, C.c_double, C.c_double,
                                        C.c_void_p]),
@@ -356,6 +380,13 @@ class Workspace:
         n = C.c_ulonglong()
         _check(self.lib.co_launch_count(self.h, C.byref(n)), "co_launch_count")
         return n.value
+
+    def set_wait_limit(self, spins: int = 0, phantom_blocks: int = 0) -> None:
+        """Bounded device-side waits (co_ctx_set_wait_limit): the LB grid
+        barrier polls at most `spins` times (0: the default) and waits for
+        `phantom_blocks` arrivals beyond the grid (0 in normal use)."""
+        _check(self.lib.co_ctx_set_wait_limit(self.h, int(spins), int(phantom_blocks)),
+               "co_ctx_set_wait_limit")
 
     def stream(self) -> int:
         """cudaStream_t (as an int) on which the context enqueues all its work."""

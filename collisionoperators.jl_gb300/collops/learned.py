@@ -1,22 +1,25 @@
 """Learned warm start of the implicit step.
 
-A small MLP (9 -> 64 -> 64 -> 64 -> 2, GELU, BF16 weights, FP32 accumulation;
+A small MLP (15 -> 64 -> 64 -> 64 -> 2, GELU, BF16 weights, FP32 accumulation;
 the kernels are this library's own, see co_mlp.cu) maps per-marker features at
-the start of a step to the normalised correction of the explicit predictor,
+the start of a step to the correction of the explicit predictor,
     delta = (v_converged - v_Euler) / dt^2,
 the form of warm start the reference planned ("Euler + dt^2 * delta" MLP
 correction, Parameters.jl:108-112; its warmstart_nn.jl is not in the tree).
+The feature and output normalisation are held by the network itself and
+applied inside its forward kernel.
 
-The fixed-point map decides: `propose` returns the learned iterate only when
-its first Picard residual (one FP32 map in the mixed forms) is smaller than
-that of the plain predictor; otherwise the predictor is used.
+The fixed-point map decides: the step starts from whichever of the learned
+proposal, the explicit predictor and the previous-step state has the smallest
+first Picard residual, and the unmodified solver judges convergence
+(co_step_learned, one C-ABI call for the whole step).
 
 Training data comes from the solver itself: `generate_pairs` runs time steps
-and records (features at the step start, delta of the converged step).
+and records (features at the step start, delta of the step) for the steps whose
+solve converged.
 """
 from __future__ import annotations
 
-import contextlib
 import ctypes as C
 
 import numpy as np
@@ -127,7 +130,14 @@ class WarmStart:
         self.xs = np.ones(self.mlp.n_in)
         self.tm = np.zeros(self.mlp.n_out)
         self.ts = np.ones(self.mlp.n_out)
-        self._xm_dev = self._xs_dev = None   # device copies of xm, xs
+
+    def _push_normalization(self) -> None:
+        """Hand the normalisation to the network: its forward kernel then takes
+        raw features and returns delta itself (co_mlp_set_normalization)."""
+        d = lambda a: np.ascontiguousarray(a, dtype=np.float64)  # noqa: E731
+        xm, xs, tm, ts = d(self.xm), d(self.xs), d(self.tm), d(self.ts)
+        _check(self.mlp.lib.co_mlp_set_normalization(self.mlp.h, _p(xm), _p(xs), _p(tm), _p(ts)),
+               "co_mlp_set_normalization")
 
     def validation_loss(self, X: np.ndarray, T: np.ndarray, device: int = 0) -> float:
         """Mean squared error of the normalised prediction on (X, T) (co_mlp_gradients
@@ -143,7 +153,6 @@ class WarmStart:
         """Train on the GPU with the library's kernels; returns the loss history."""
         import torch
         self.xm, self.xs = X.mean(0), X.std(0) + 1e-12
-        self._xm_dev = None
         self.tm, self.ts = T.mean(0), T.std(0) + 1e-30
         Xn = torch.from_numpy(((X - self.xm) / self.xs).astype(np.float32)).cuda(device)
         Tn = torch.from_numpy(((T - self.tm) / self.ts).astype(np.float32)).cuda(device)
@@ -159,21 +168,16 @@ class WarmStart:
                                            lr * (0.5 ** (ep // max(1, epochs // 3))))
                 cnt += 1
             hist.append(tot / max(cnt, 1))
+        self._push_normalization()
         return hist
 
     def predict_delta(self, X, stream: int = 0):
-        """Normalised features -> delta (float32 CUDA tensors). With `stream` set,
-        the normalisation and the network run on that stream."""
+        """Raw features (float32 CUDA tensor (B, 15)) -> delta (B, 2), both the
+        normalisation and the network in the library's forward kernel, on
+        `stream` (a cudaStream_t as an int)."""
         import torch
-        ctx = (torch.cuda.stream(torch.cuda.ExternalStream(stream, device=X.device))
-               if stream else contextlib.nullcontext())
-        with ctx:
-            if self._xm_dev is None or self._xm_dev.device != X.device:
-                self._xm_dev = torch.from_numpy(self.xm.astype(np.float32)).to(X.device)
-                self._xs_dev = torch.from_numpy(self.xs.astype(np.float32)).to(X.device)
-            Xn = ((X - self._xm_dev) / self._xs_dev).contiguous()
-            Y = torch.empty((X.shape[0], N_OUT), dtype=torch.float32, device=X.device)
-            self.mlp.forward(Xn, Y, stream)
+        Y = torch.empty((X.shape[0], N_OUT), dtype=torch.float32, device=X.device)
+        self.mlp.forward(X.contiguous(), Y, stream)
         return Y
 
     def propose(self, ws: Workspace, opts: CoOpts, v, w, S0: float, dt: float, v1_out,
@@ -189,8 +193,8 @@ class WarmStart:
         Y = self.predict_delta(X, ws.stream())
         N = v.shape[1]
         vl = torch.empty_like(v)
-        sc = np.ascontiguousarray(self.ts, dtype=np.float64)
-        sh = np.ascontiguousarray(self.tm, dtype=np.float64)
+        sc = np.ones(N_OUT)       # the network returns delta itself
+        sh = np.zeros(N_OUT)
         _check(ws.lib.co_warmstart_apply_dev(ws.h, vp.data_ptr(), Y.data_ptr(), N, dt, _p(sc),
                                              _p(sh), vl.data_ptr()), "co_warmstart_apply_dev")
         rl = C.c_double()
@@ -218,52 +222,44 @@ class WarmStart:
                                "collops.train_warmstart")
         ws.mlp.set_params(z["params"])
         ws.xm, ws.xs, ws.tm, ws.ts = z["xm"], z["xs"], z["tm"], z["ts"]
-        ws._xm_dev = None
+        ws._push_normalization()
         return ws
+
+    def step(self, ws: Workspace, opts: CoOpts, dopt, x, w, S0: float, dt: float, v_new,
+             retry: bool = True, use_network: bool = True) -> dict:
+        """One whole time step through co_step_learned_dev: the start with the
+        smallest first residual among the learned proposal, the explicit
+        predictor and the previous-step state, the implicit solve (dopt: defect
+        correction; None: step_anderson!), one retry from the next start if it
+        does not converge, and the entropy of the new state. x, w, v_new are
+        torch CUDA tensors ((2, N), (N,), (2, N)); returns the step record."""
+        from . import CoStepInfo
+        info = CoStepInfo()
+        N = x.shape[1]
+        _check(ws.lib.co_step_learned_dev(ws.h, C.byref(opts),
+                                          C.byref(dopt) if dopt is not None else None,
+                                          self.mlp.h if use_network else None, int(retry),
+                                          v_new.data_ptr(), x.data_ptr(), w.data_ptr(), N, S0, dt,
+                                          C.byref(info)), "co_step_learned_dev")
+        return info.as_dict()
 
 
 def step_defect_warm(ws: Workspace, warm: "WarmStart", opts: CoOpts, dopt, x, w, S0: float,
                      dt: float, v1, retry: bool = True):
-    """One implicit step from x (torch (2, N)) by defect correction
-    (co_step_defect_dev) started from the learned warm start. When the solve
-    from the chosen start stagnates above the tolerance, it is solved once more
-    from the other candidate (predictor or learned proposal) and the better of
-    the two results is kept. v1 receives the new markers. Returns
-    (outer, residual, inner, r0) of the kept solve and a record of the
-    proposal and the attempts."""
-    import torch
-    alt = torch.empty_like(x)
-    used, rl, rp = warm.propose(ws, opts, x, w, S0, dt, v1, alt)
-    N = x.shape[1]
-
-    def solve(start):
-        it, inner = C.c_int(), C.c_int()
-        res, r0 = C.c_double(), C.c_double()
-        _check(ws.lib.co_step_defect_dev(ws.h, C.byref(opts), C.byref(dopt), start.data_ptr(),
-                                         x.data_ptr(), w.data_ptr(), N, S0, dt, C.byref(it),
-                                         C.byref(res), C.byref(inner), C.byref(r0)),
-               "co_step_defect_dev")
-        return (it.value, res.value, inner.value, r0.value)
-
-    info = solve(v1)
-    rec = dict(used_learned=bool(used), r_learned=rl, r_predictor=rp, attempts=1)
-    if retry and not info[1] < opts.tol * float(torch.linalg.vector_norm(v1)):
-        info2 = solve(alt)
-        rec["attempts"] = 2
-        if info2[1] < info[1]:
-            v1.copy_(alt)
-            info = (info[0] + info2[0], info2[1], info[2] + info2[2], info[3])
-            rec["kept"] = "retry"
-        else:
-            info = (info[0] + info2[0], info[1], info[2] + info2[2], info[3])
-            rec["kept"] = "first"
-    return info, rec
+    """One implicit step from x (torch (2, N)) by defect correction from the
+    learned warm start (WarmStart.step, i.e. co_step_learned_dev). v1 receives
+    the new markers. Returns (outer, residual, inner, r0) and the step record."""
+    rec = warm.step(ws, opts, dopt, x, w, S0, dt, v1, retry=retry)
+    return (rec["outer"], rec["res"], rec["inner"], rec["r0"]), rec
 
 
 def generate_pairs(ws: Workspace, opts: CoOpts, v, w, dt: float, steps: int, solve):
     """Run `steps` time steps from v (torch (2, N)); `solve(v1, v, S0)` performs
-    the implicit step in place on v1. Returns (X, T) numpy arrays: features at
-    each step start and delta = (v_converged - v_pred)/dt^2, plus the final v."""
+    the implicit step in place on v1 and returns True when it converged.
+    Returns (X, T, x): features at each converged step's start and delta =
+    (v_converged - v_pred)/dt^2 as numpy arrays (steps whose solve did not
+    converge are advanced but not kept: their delta is not a fixed point), and
+    the final state."""
     import torch
     Xs, Ts = [], []
     x = v.clone()
@@ -271,11 +267,15 @@ def generate_pairs(ws: Workspace, opts: CoOpts, v, w, dt: float, steps: int, sol
         S0 = entropy_of(ws, x, w)
         X, vp, _rp = features(ws, opts, x, w, S0, dt)
         v1 = vp.clone()
-        solve(v1, x, S0)
-        delta = ((v1 - vp) / (dt * dt)).T.contiguous()
-        Xs.append(X.cpu().numpy())
-        Ts.append(delta.cpu().numpy())
+        ok = solve(v1, x, S0)
+        if ok is None or ok:
+            delta = ((v1 - vp) / (dt * dt)).T.contiguous()
+            Xs.append(X.cpu().numpy())
+            Ts.append(delta.cpu().numpy())
         x = v1
+    if not Xs:
+        n = N_IN
+        return np.zeros((0, n), np.float32), np.zeros((0, N_OUT), np.float32), x
     return np.concatenate(Xs), np.concatenate(Ts), x
 
 

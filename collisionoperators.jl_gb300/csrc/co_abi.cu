@@ -182,6 +182,7 @@ static void free_ctx(co_ctx *c) {
                     c->mb.Adef, c->mb.aa, c->mb.pc, c->st2, c->st3};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    co_step_free(c);
     co_prof_free(c);
     if (c->st_host) cudaFreeHost(c->st_host);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -301,6 +302,13 @@ extern "C" int co_ctx_destroy(co_ctx *c) {
 extern "C" int co_ctx_n_dofs(const co_ctx *c, int *n) {
     if (!c || !n) return CO_ERR_ARG;
     *n = c->n_dofs;
+    return CO_OK;
+}
+
+extern "C" int co_ctx_set_wait_limit(co_ctx *c, int spins, int phantom_blocks) {
+    if (!c || phantom_blocks < 0) return CO_ERR_ARG;
+    c->barrier_spins = spins > 0 ? spins : 0;
+    c->barrier_phantom = phantom_blocks;
     return CO_OK;
 }
 

@@ -120,6 +120,11 @@ struct co_ctx {
     // batch membership (co_batch): marker count and whether the instance has a pair sum
     int batch_N, batch_landau;
     int lb_two_pass;          // LB drift in two launches (capturable) instead of cooperative
+    // bounded grid barrier of the cooperative LB kernel: polls before it gives
+    // up with CO_ERR_TIMEOUT, and phantom blocks it waits for on top of the
+    // grid (0 in normal use; a test sets 1 so that the barrier cannot complete)
+    int barrier_spins, barrier_phantom;
+    struct co_step_bufs *sb;  // buffers of co_step_learned (co_step.cu), allocated on first use
 };
 
 // ------------------------------------------------------------- helpers
@@ -166,6 +171,7 @@ int co_predictor_buffers(co_ctx *c, const co_opts *o, int precision, const doubl
 void co_ctx_destroy_detached(co_ctx *c);   // free a context whose stream/state it does not own
 int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *dopt, int N,
                            double S0, double dt, int *outer, double *res, int *inner, double *r0);
+void co_step_free(co_ctx *c);           // co_step.cu
 #define CO_PREC_BOTH 3                  // pack both FP64 and FP32 operands (internal)
 // packed-operand sets a precision needs: 1 = FP64 arrays, 2 = FP32 head/tail arrays
 static inline int co_pack_mode(int precision) {

@@ -45,7 +45,12 @@ struct co_mlp {
     float *y;                    // B x n_out outputs
     float *d;                    // B x (3 H + n_out) deltas
     int cap;
+    // feature and output normalisation applied by co_mlp_forward (inference):
+    // [mean (MLP_MAX_IN), 1/std (MLP_MAX_IN), out std (MLP_MAX_OUT), out mean
+    // (MLP_MAX_OUT)]; NULL = none. Training kernels see normalised data as given.
+    float *norm;
 };
+#define MLP_NORM_FLOATS (2 * MLP_MAX_IN + 2 * MLP_MAX_OUT)
 
 // parameter offsets: W0 [H][n_in], b0 [H], W1 [H][H], b1 [H], W2 [H][H], b2 [H],
 // W3 [n_out][H], b3 [n_out]
@@ -126,7 +131,7 @@ __device__ __forceinline__ void mlp_fwd(const float *sp, mlp_off o, int n_in, in
 __global__ void __launch_bounds__(MLP_TPB)
 k_mlp_forward(const __nv_bfloat16 *__restrict__ wbf, const float *__restrict__ master, int n_in,
               int n_out, const float *__restrict__ X, int B, float *__restrict__ Y,
-              float *__restrict__ Z) {
+              float *__restrict__ Z, const float *__restrict__ norm) {
     extern __shared__ float sp[];
     mlp_off o = mlp_offsets(n_in, n_out);
     mlp_load(wbf, master, o, n_in, n_out, sp);
@@ -134,11 +139,19 @@ k_mlp_forward(const __nv_bfloat16 *__restrict__ wbf, const float *__restrict__ m
     if (s >= B) return;
     float x[MLP_MAX_IN], out[MLP_MAX_OUT];
 #pragma unroll
-    for (int i = 0; i < MLP_MAX_IN; i++) x[i] = i < n_in ? X[(size_t)s * n_in + i] : 0.f;
+    for (int i = 0; i < MLP_MAX_IN; i++) {
+        float xi = i < n_in ? X[(size_t)s * n_in + i] : 0.f;
+        if (norm && i < n_in) xi = (xi - norm[i]) * norm[MLP_MAX_IN + i];
+        x[i] = xi;
+    }
     mlp_fwd(sp, o, n_in, n_out, x, Z ? Z + (size_t)s * 3 * MLP_H : nullptr, out);
 #pragma unroll
     for (int k = 0; k < MLP_MAX_OUT; k++)
-        if (k < n_out) Y[(size_t)s * n_out + k] = out[k];
+        if (k < n_out) {
+            float y = out[k];
+            if (norm) y = fmaf(y, norm[2 * MLP_MAX_IN + k], norm[2 * MLP_MAX_IN + MLP_MAX_OUT + k]);
+            Y[(size_t)s * n_out + k] = y;
+        }
 }
 
 // per-sample deltas: D[s] = [dz0 (H), dz1 (H), dz2 (H), dy (n_out)]
@@ -318,7 +331,7 @@ extern "C" int co_mlp_create(int n_in, int n_out, unsigned seed, int device, co_
 extern "C" int co_mlp_destroy(co_mlp *m) {
     if (!m) return CO_ERR_ARG;
     cudaSetDevice(m->device);
-    void *ptrs[] = {m->master, m->wbf, m->grad, m->m1, m->m2, m->z, m->y, m->d};
+    void *ptrs[] = {m->master, m->wbf, m->grad, m->m1, m->m2, m->z, m->y, m->d, m->norm};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     free(m);
@@ -350,14 +363,41 @@ extern "C" int co_mlp_get_params(const co_mlp *m, float *host) {
     return CO_OK;
 }
 
-// Y = net(X) for B samples (device pointers, row-major B x n_in / B x n_out)
+extern "C" int co_mlp_set_normalization(co_mlp *m, const double *x_mean, const double *x_std,
+                                        const double *y_mean, const double *y_std) {
+    if (!m) return CO_ERR_ARG;
+    CO_CK(cudaSetDevice(m->device));
+    if (!x_mean) {
+        if (m->norm) cudaFree(m->norm);
+        m->norm = nullptr;
+        return CO_OK;
+    }
+    if (!x_std || !y_mean || !y_std) return CO_ERR_ARG;
+    float h[MLP_NORM_FLOATS] = {0.f};
+    for (int i = 0; i < m->n_in; i++) {
+        if (!(x_std[i] > 0.0) || !isfinite(x_mean[i])) return CO_ERR_ARG;
+        h[i] = (float)x_mean[i];
+        h[MLP_MAX_IN + i] = (float)(1.0 / x_std[i]);
+    }
+    for (int k = 0; k < m->n_out; k++) {
+        if (!isfinite(y_std[k]) || !isfinite(y_mean[k])) return CO_ERR_ARG;
+        h[2 * MLP_MAX_IN + k] = (float)y_std[k];
+        h[2 * MLP_MAX_IN + MLP_MAX_OUT + k] = (float)y_mean[k];
+    }
+    if (!m->norm && cudaMalloc(&m->norm, sizeof(h)) != cudaSuccess) return CO_ERR_NOMEM;
+    CO_CK(cudaMemcpy(m->norm, h, sizeof(h), cudaMemcpyHostToDevice));
+    return CO_OK;
+}
+
+// Y = net(X) for B samples (device pointers, row-major B x n_in / B x n_out),
+// with the normalisation of co_mlp_set_normalization applied if set
 extern "C" int co_mlp_forward(co_mlp *m, const float *X, int B, float *Y, void *stream) {
     if (!m || B < 0 || (B > 0 && (!X || !Y))) return CO_ERR_ARG;
     if (B == 0) return CO_OK;
     CO_CK(cudaSetDevice(m->device));
     int smem = (int)(sizeof(float) * m->P);
     k_mlp_forward<<<co_cdiv(B, MLP_TPB), MLP_TPB, smem, (cudaStream_t)stream>>>(
-        m->wbf, m->master, m->n_in, m->n_out, X, B, Y, nullptr);
+        m->wbf, m->master, m->n_in, m->n_out, X, B, Y, nullptr, m->norm);
     CO_CK(cudaGetLastError());
     return CO_OK;
 }
@@ -367,7 +407,7 @@ static int mlp_grad(co_mlp *m, const float *X, const float *T, int B, float *los
     if (rc) return rc;
     int smem = (int)(sizeof(float) * m->P);
     k_mlp_forward<<<co_cdiv(B, MLP_TPB), MLP_TPB, smem>>>(m->wbf, m->master, m->n_in, m->n_out, X,
-                                                         B, m->y, m->z);
+                                                         B, m->y, m->z, nullptr);
     k_mlp_backward<<<co_cdiv(B, MLP_TPB), MLP_TPB, smem>>>(m->wbf, m->master, m->n_in, m->n_out,
                                                           m->z, m->y, T, B, m->d);
     k_mlp_wgrad<<<co_cdiv(m->P, 128), 128>>>(m->n_in, m->n_out, X, m->z, m->d, B, m->grad);

@@ -18,10 +18,15 @@
 //     first call before any stream capture.
 //   - All calls share the one array. Every partial the reduction reads is
 //     written earlier in the same call, so leftover contents of a previous call
-//     are never read and nothing has to be cleared; but two calls whose kernels
-//     overlap on the GPU (different streams, or different host threads) race on
-//     the array and must be serialised by the caller.
-//   - The work is enqueued on the caller's stream and not synchronised.
+//     are never read; the one word that must start at zero (the non-finite
+//     flag) is cleared by each call. Two calls whose kernels overlap on the GPU
+//     (different streams, or different host threads) race on the array and must
+//     be serialised by the caller.
+//   - Inputs are checked for NaN/Inf first, on the GPU: the call waits for that
+//     check (and so for the work queued before it on the caller's stream) and
+//     returns CO_ERR_NONFINITE without touching dot_v if one is found, as the
+//     context entry points do. The pair sum itself is then enqueued on the
+//     caller's stream and not synchronised.
 //
 // Arithmetic: one-sided FP64 pair loop with the reference's masks (targets
 // outside (bp[1], bp[end]) get 0, sources outside are skipped, |d|^2 < 1e-24
@@ -36,8 +41,10 @@
 #define NA_TPB 128
 #define NA_R2_MIN_BITS 0x3B282DB34012B251LL  // bit pattern of 1e-24
 
-// 8 slices x 2 components x 32768 markers of FP64 = 4 MiB per device
-static __device__ __align__(256) double g_noalloc_part[CO_NOALLOC_SLICES * 2 * CO_NOALLOC_MAX_N];
+// 8 slices x 2 components x 32768 markers of FP64 = 4 MiB per device, then a
+// 256-byte tail whose first word is the non-finite flag of the current call
+#define CO_NOALLOC_PART (CO_NOALLOC_SLICES * 2 * CO_NOALLOC_MAX_N)
+static __device__ __align__(256) double g_noalloc_part[CO_NOALLOC_PART + 32];
 
 static std::mutex g_noalloc_mu;
 static double *g_noalloc_addr[64];  // device address of g_noalloc_part, per device
@@ -126,6 +133,17 @@ k_noalloc_pair(const double *__restrict__ v, const double *__restrict__ w,
     }
 }
 
+// flag = 1 if any of v (2N), w (N), G (2N) is NaN or Inf
+__global__ void k_noalloc_check(const double *__restrict__ v, const double *__restrict__ w,
+                                const double *__restrict__ G, int N, unsigned *flag) {
+    int bad = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+        bad |= !isfinite(v[i]) | !isfinite(v[N + i]) | !isfinite(w[i]) | !isfinite(G[i]) |
+               !isfinite(G[N + i]);
+    }
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flag, 1u);
+}
+
 __global__ void k_noalloc_reduce(const double *__restrict__ part, int N, int split,
                                  double *__restrict__ dot_v) {
     int g = blockIdx.x * blockDim.x + threadIdx.x;
@@ -165,6 +183,15 @@ extern "C" int co_collision_noalloc(const double *v, const double *w, const doub
     int rc = noalloc_scratch(&part);
     if (rc) return rc;
     cudaStream_t s = (cudaStream_t)stream;
+    unsigned *flag = (unsigned *)(part + CO_NOALLOC_PART);
+    unsigned bad = 0;
+    CO_CK(cudaMemsetAsync(flag, 0, sizeof(unsigned), s));
+    k_noalloc_check<<<co_cdiv(N, 256) < 304 ? co_cdiv(N, 256) : 304, 256, 0, s>>>(v, w, G, N,
+                                                                                flag);
+    CO_CK(cudaGetLastError());
+    CO_CK(cudaMemcpyAsync(&bad, flag, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    CO_CK(cudaStreamSynchronize(s));
+    if (bad) return CO_ERR_NONFINITE;
     const int tiles = co_cdiv(N, NA_TPB);
     int split = co_cdiv(608, tiles);  // about 4 blocks per SM on 152 SMs
     if (split > CO_NOALLOC_SLICES) split = CO_NOALLOC_SLICES;

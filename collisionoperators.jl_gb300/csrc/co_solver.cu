@@ -68,9 +68,12 @@ k_lambda(const double *__restrict__ red, int nred, co_solver_state *st, double S
 // ---------------------------------------------------------------- LB fused
 
 // Grid barrier for a cooperative launch (all blocks co-resident). The wait is
-// bounded: after CO_BARRIER_SPINS polls the block records a timeout in *err
-// and continues, so the kernel always terminates.
-__device__ __forceinline__ void grid_barrier(unsigned *counter, unsigned nblocks, int *err) {
+// bounded: after max_spins polls (CO_BARRIER_SPINS unless a test lowers it)
+// the block records a timeout in *err and continues, so the kernel always
+// terminates. nblocks is the number of arrivals the barrier waits for: the
+// grid size, or more when a test asks for a barrier that cannot complete.
+__device__ __forceinline__ void grid_barrier(unsigned *counter, unsigned nblocks, int *err,
+                                             int max_spins) {
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
@@ -78,7 +81,7 @@ __device__ __forceinline__ void grid_barrier(unsigned *counter, unsigned nblocks
         unsigned target = (old / nblocks + 1u) * nblocks;
         int spins = 0;
         while (*((volatile unsigned *)counter) < target) {
-            if (++spins > CO_BARRIER_SPINS) {
+            if (++spins > max_spins) {
                 atomicExch(err, 1);
                 break;
             }
@@ -120,7 +123,8 @@ k_lb_fused(int N, const double *__restrict__ vmid, const double *__restrict__ w,
            double *__restrict__ g, const double *__restrict__ dv, int use_lambda, double nu,
            double dt, const double *__restrict__ v0, double *__restrict__ Gv,
            const double *__restrict__ v1, double *__restrict__ r, double *__restrict__ red7,
-           double *__restrict__ red2, co_solver_state *st, unsigned *bar, int *err) {
+           double *__restrict__ red2, co_solver_state *st, unsigned *bar, int *err,
+           unsigned bar_blocks, int bar_spins) {
     __shared__ double sh[32];
     __shared__ double sol[3];
     const double lam = use_lambda ? st->lambda : 0.0;
@@ -148,7 +152,7 @@ k_lb_fused(int N, const double *__restrict__ vmid, const double *__restrict__ w,
         double s = co_block_sum(m[k], sh);
         if (threadIdx.x == 0) red7[blockIdx.x * 8 + k] = s;
     }
-    grid_barrier(bar, gridDim.x, err);
+    grid_barrier(bar, bar_blocks, err, bar_spins);
     if (threadIdx.x == 0 && *((volatile int *)err)) st->error = CO_ERR_TIMEOUT;
     // every block reduces the partials in the same fixed order
     double tot[7];
@@ -574,8 +578,10 @@ int co_lb_fused(co_ctx *c, int N, double nu, double dt, double *Gv, const double
     double *red7 = c->mb.red + (size_t)c->mb.red_cap * 8;  // disjoint from red2 (first 2*grid)
     double *red2 = c->mb.red;
     int use_lambda = gonzalez;
+    unsigned bar_blocks = (unsigned)(grid + (c->barrier_phantom > 0 ? c->barrier_phantom : 0));
+    int bar_spins = c->barrier_spins > 0 ? c->barrier_spins : CO_BARRIER_SPINS;
     void *args[] = {&N, &vmid, &w, &g, &dv, &use_lambda, &nu, &dt, &v0, &Gv, &v1, &r,
-                    &red7, &red2, &c->st, &bar, &err};
+                    &red7, &red2, &c->st, &bar, &err, &bar_blocks, &bar_spins};
     CO_CK(cudaLaunchCooperativeKernel((void *)k_lb_fused, grid, CO_RED_THREADS, args, 0,
                                       c->stream));
     c->launches++;

@@ -233,8 +233,11 @@ int co_entropy_of_markers_dev(co_ctx *ctx, const double *v, const double *w,
  * exit. N must be <= 32768 (else CO_ERR_SIZE). The first call on a device sets
  * up the array's address and should come before any stream capture. All calls
  * share the array: calls whose kernels overlap on the GPU race and must be
- * serialised by the caller. Work is enqueued on `stream` (a cudaStream_t, NULL
- * for the default stream) and not synchronised. FP64, one-sided pair loop. */
+ * serialised by the caller. The inputs are first checked for NaN/Inf on the
+ * GPU; the call waits for that check on `stream` (a cudaStream_t, NULL for the
+ * default stream) and returns CO_ERR_NONFINITE, with dot_v untouched, if one
+ * is found. The pair sum is then enqueued on `stream` and not synchronised.
+ * FP64, one-sided pair loop. */
 int co_collision_noalloc(const double *v, const double *w, const double *G,
                          double *dot_v, int N, double lo1, double hi1, double lo2,
                          double hi2, void *stream);
@@ -312,6 +315,58 @@ int co_warmstart_apply_dev(co_ctx *ctx, const double *v_pred, const float *Y, in
 int co_picard_residual_dev(co_ctx *ctx, const co_opts *opts, const double *v_in,
                            const double *v0, const double *w, int N, double S0, double dt,
                            double *res);
+
+/* Feature and output normalisation of the network, applied by co_mlp_forward
+ * (inference only; training kernels take the data as given): inputs become
+ * (x - x_mean) / x_std, outputs y * y_std + y_mean. Host arrays of n_in, n_in,
+ * n_out, n_out values; x_mean = NULL removes the normalisation. */
+int co_mlp_set_normalization(co_mlp *mlp, const double *x_mean, const double *x_std,
+                             const double *y_mean, const double *y_std);
+
+/* Record of one co_step_learned time step. */
+typedef struct {
+    int outer;            /* outer maps (defect) or iterations (Anderson), all attempts */
+    int inner;            /* inner maps of the defect correction, all attempts          */
+    double res;           /* residual of the kept solve (its best, if it stagnated)     */
+    double r0;            /* initial residual of the kept solve                         */
+    int converged;        /* the kept solve met max(tol ||v||, abs_floor)               */
+    int exit;             /* 1 converged, 2 stagnation exit (solver.jl:357-367),
+                             3 iteration cap (solver.jl:419-422)                        */
+    int start;            /* start of the kept solve: 0 explicit predictor, 1 learned
+                             proposal, 2 previous-step state                            */
+    int attempts;         /* 2 when a non-converged solve was repeated from the next start */
+    double r_start[3];    /* first residuals ||G(x) - x|| of the three starts (predictor,
+                             learned, previous state; learned = +inf without a network) */
+    double S_new;         /* entropy of the new state's projection: the next step's S0  */
+} co_step_info;
+
+/* One whole time step of the reference's loop (main.jl:233-271: predictor,
+ * network correction nn_warmstart_correct! at :252-254, implicit solve) on the
+ * device. Starts: the explicit predictor, the learned proposal v_pred + dt^2 *
+ * mlp(features) (mlp carries its normalisation; NULL: no proposal) and the
+ * previous-step state v. The solve (dopts != NULL: step_defect!, else
+ * step_anderson!, in opts->precision) starts from the candidate with the
+ * smallest first residual of the unmodified map (FP32 pair maps in the mixed
+ * forms); with retry != 0 a solve that does not converge is repeated once from
+ * the next candidate and the smaller residual is kept. v_new receives the new
+ * markers, info the record. co_step_learned takes HOST arrays (copies in and
+ * out inside the call); co_step_learned_dev device arrays. */
+int co_step_learned(co_ctx *ctx, const co_opts *opts, const co_defect_opts *dopts,
+                    co_mlp *mlp, int retry, double *v_new, const double *v,
+                    const double *w, int N, double S0, double dt, co_step_info *info);
+int co_step_learned_dev(co_ctx *ctx, const co_opts *opts, const co_defect_opts *dopts,
+                        co_mlp *mlp, int retry, double *v_new, const double *v,
+                        const double *w, int N, double S0, double dt, co_step_info *info);
+
+/* Limits of the context's bounded device-side waits (no counterpart in the
+ * reference, whose GPU code never waits on the device). The LB drift kernel
+ * reduces its moments across the grid through a barrier that polls at most
+ * `spins` times (about 64 ns each; <= 0 selects the default of 2^22) and then
+ * gives up: the kernel finishes and the call returns CO_ERR_TIMEOUT, leaving
+ * the context usable. `phantom_blocks` (0 in normal use) adds arrivals the
+ * barrier waits for; a failure-path test sets 1, so that the barrier cannot
+ * complete and the timeout path runs without any fault. */
+int co_ctx_set_wait_limit(co_ctx *ctx, int spins, int phantom_blocks);
 
 /* Number of kernels this context has launched so far. */
 int co_launch_count(const co_ctx *ctx, unsigned long long *launches);

@@ -49,6 +49,7 @@ def _load():
     lib.om_extraction.argtypes = [C.c_void_p, C.c_int, _dp]
     lib.om_quadrature.argtypes = [C.c_void_p, _dp, _dp]
     lib.om_mass_solve.argtypes = [C.c_void_p, _dp, _dp]
+    lib.om_set_mass_solver.argtypes = [C.c_void_p, C.c_int]
     lib.om_l2_project.argtypes = [C.c_void_p, _dp, _dp, C.c_int, _dp]
     lib.om_l2_rhs.argtypes = [C.c_void_p, _dp, _dp, C.c_int, _dp]
     lib.om_compute_r.argtypes = [C.c_void_p, _dp, _dp]
@@ -168,6 +169,11 @@ class OracleMesh:
         w = np.zeros(self.nquad)
         self.lib.om_quadrature(self.h, _d(x), _d(w))
         return x, w
+
+    def set_mass_solver(self, kind: int) -> None:
+        """0: 2D banded Cholesky (default); 1: tensor-product solve with the 1D
+        Cholesky factors -- a second correct FP64 solve for round-off studies."""
+        self.lib.om_set_mass_solver(self.h, int(kind))
 
     def mass_solve(self, rhs) -> np.ndarray:
         rhs = np.ascontiguousarray(rhs, dtype=np.float64)

@@ -40,6 +40,10 @@ struct om_mesh {
     int bw;              /* half bandwidth of the 2D mass matrix */
     double *Lb;          /* banded Cholesky factor, row i: cols i-bw..i */
     int use_logsq;
+    int mass_kind;       /* 0: 2D banded Cholesky (default); 1: tensor-product
+                            solve with the 1D factors below                      */
+    double *L1, *L2;     /* banded Cholesky factors of the 1D mass matrices,
+                            row i: cols i-2..i (5-diagonal matrices)            */
 };
 
 /* ---------------------------------------------------------------- quadrature */
@@ -233,8 +237,71 @@ static void assemble_mass_band(om_mesh *m) {
     m->Lb = A;
 }
 
+/* 1D mass matrix of dimension d (3-point GL per element, the same rule as the
+ * 2D assembly, of which M = M2 (x) M1 is the Kronecker product) and its banded
+ * Cholesky factor, half bandwidth 2. */
+static double *mass1d_factor(const double *bp, int n, const double *C) {
+    int nd = n + 2;
+    double *A = calloc((size_t)nd * 3, sizeof(double)); /* A[i][2 - (i-j)] */
+    double gx[3], gw[3];
+    gauss_legendre01(3, gx, gw);
+    for (int e = 0; e < n; e++) {
+        double h = bp[e + 1] - bp[e];
+        for (int q = 0; q < 3; q++) {
+            double B[3], p[3];
+            bern2(gx[q], B, NULL);
+            extract3(C + 9 * e, B, p);
+            for (int a = 0; a < 3; a++)
+                for (int b = 0; b <= a; b++)
+                    A[(size_t)(e + a) * 3 + (2 - (a - b))] += p[a] * p[b] * gw[q] * h;
+        }
+    }
+    for (int i = 0; i < nd; i++) {
+        int j0 = i - 2 < 0 ? 0 : i - 2;
+        for (int j = j0; j <= i; j++) {
+            double s = A[(size_t)i * 3 + (2 - (i - j))];
+            int k0 = j - 2 > j0 ? j - 2 : j0;
+            for (int k = k0; k < j; k++)
+                s -= A[(size_t)i * 3 + (2 - (i - k))] * A[(size_t)j * 3 + (2 - (j - k))];
+            if (j == i) A[(size_t)i * 3 + 2] = sqrt(s);
+            else A[(size_t)i * 3 + (2 - (i - j))] = s / A[(size_t)j * 3 + 2];
+        }
+    }
+    return A;
+}
+
+/* x <- M^{-1} x for one line of a 1D factor L (length nd, stride st) */
+static void line_solve(const double *L, int nd, double *x, size_t st) {
+    for (int i = 0; i < nd; i++) {
+        double s = x[i * st];
+        for (int k = (i - 2 < 0 ? 0 : i - 2); k < i; k++) s -= L[(size_t)i * 3 + (2 - (i - k))] * x[k * st];
+        x[i * st] = s / L[(size_t)i * 3 + 2];
+    }
+    for (int i = nd - 1; i >= 0; i--) {
+        double s = x[i * st];
+        for (int k = i + 1; k <= (i + 2 < nd ? i + 2 : nd - 1); k++)
+            s -= L[(size_t)k * 3 + (2 - (k - i))] * x[k * st];
+        x[i * st] = s / L[(size_t)i * 3 + 2];
+    }
+}
+
+void om_set_mass_solver(om_mesh *m, int kind) {
+    m->mass_kind = kind == 1 ? 1 : 0;
+    if (m->mass_kind == 1 && !m->L1) {
+        m->L1 = mass1d_factor(m->bp1, m->n1, m->C1);
+        m->L2 = mass1d_factor(m->bp2, m->n2, m->C2);
+    }
+}
+
 void om_mass_solve(const om_mesh *m, const double *rhs, double *out) {
     int nd = m->n_dofs, bw = m->bw;
+    if (m->mass_kind == 1) {
+        /* M = M2 (x) M1 with index i1 + i2 nd1: solve along i1, then along i2 */
+        memcpy(out, rhs, sizeof(double) * nd);
+        for (int i2 = 0; i2 < m->nd2; i2++) line_solve(m->L1, m->nd1, out + (size_t)i2 * m->nd1, 1);
+        for (int i1 = 0; i1 < m->nd1; i1++) line_solve(m->L2, m->nd2, out + i1, m->nd1);
+        return;
+    }
     const double *A = m->Lb;
     double *y = malloc(sizeof(double) * nd);
     for (int i = 0; i < nd; i++) {
@@ -300,6 +367,7 @@ om_mesh *om_create(const double *bp1, int nb1, const double *bp2, int nb2,
 void om_destroy(om_mesh *m) {
     if (!m) return;
     free(m->bp1); free(m->bp2); free(m->C1); free(m->C2); free(m->Lb);
+    free(m->L1); free(m->L2);
     free(m);
 }
 

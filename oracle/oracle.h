@@ -40,6 +40,12 @@ void om_extraction(const om_mesh *m, int dim, double *out);
 /* GL nodes/weights on [0,1] used for r and S. */
 void om_quadrature(const om_mesh *m, double *x, double *w);
 
+/* Mass-solve variant used by every later call: 0 = 2D banded Cholesky of the
+ * assembled matrix (default); 1 = the tensor-product solve M^{-1} = M2^{-1} (x)
+ * M1^{-1} with banded Cholesky factors of the 1D matrices. Both are correct FP64
+ * solves; comparing results of the two measures how far FP64 round-off of the
+ * solve alone moves a downstream quantity. */
+void om_set_mass_solver(om_mesh *m, int kind);
 /* ldiv!(out, M_lu, rhs)  (solver.jl:67) */
 void om_mass_solve(const om_mesh *m, const double *rhs, double *out);
 /* l2_project!  (functions.jl:121-134) */

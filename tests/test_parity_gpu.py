@@ -6,12 +6,11 @@ Tolerances:
     <= 1e-12 * max-abs of the oracle value (normwise relative).
   - Picard map velocities: ||v_out^gpu - v_out^oracle||_inf /
     ||v_out^oracle||_inf <= 1e-12 (the per-RHS bar of the FP64 form).
-  - LB velocities: 1e-11. The LB drift uses g = grad f_s / f_s
-    (functions.jl:37-64), which multiplies the FP64 round-off of f_s by
-    1/f_s where f_s is small (tails, Gibbs undershoot); two correct FP64
-    evaluations of f_s (banded Cholesky on the host vs. the tensor-product
-    inverse on the device) then differ there by more than 1e-12 of max|v|.
-    The reference's own GPU path (atomic scatter) has the same sensitivity.
+  - LB velocities: the same 1e-12. g = grad f_s / f_s (functions.jl:37-64)
+    multiplies the FP64 round-off of f_s by 1/f_s in the tails; two correct
+    FP64 mass solves in the oracle (2D banded Cholesky and the tensor-product
+    1D solve) move the LB map by 8e-14 (C1) and 4e-15 (C2) relative, so the
+    per-RHS bar holds with room (test_oracle.py::test_two_mass_solves_spread).
   - Mixed FP32 pair sum: normwise relative 1e-5 on vdot.
 """
 from __future__ import annotations
@@ -24,7 +23,7 @@ from conftest import gaussian_markers, uniform_bp
 pytestmark = pytest.mark.gpu
 
 TOL64 = 1e-12
-TOL_LB = 1e-11
+TOL_LB = TOL64
 
 
 def rel(a, b):
