@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "collops", "_lib")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libcollops.so")
-SOURCES = ["co_spline.cu", "co_pair.cu", "co_solver.cu", "co_abi.cu", "co_prof.cu", "co_noalloc.cu", "co_mlp.cu", "co_step.cu"]
+SOURCES = ["co_spline.cu", "co_pair.cu", "co_solver.cu", "co_abi.cu", "co_prof.cu", "co_noalloc.cu", "co_mlp.cu", "co_step.cu", "co_newton.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
          "-Xptxas", "-O3"]

@@ -24,7 +24,8 @@ __all__ = [
     "compute_collision_gpu", "compute_collision_gpu32", "compute_collision_metric_gpu",
     "l2_project_gpu", "compute_G_gpu", "eval_loggrad_gpu", "compute_r_gpu",
     "compute_entropy_gpu", "mass_solve_gpu", "picard_map", "step_anderson", "step_defect",
-    "predictor",
+    "step_newton",
+    "predictor", "save_checkpoint", "load_checkpoint", "checkpoint_path",
     "enable_gpu", "Hooks", "library_path", "load_library",
 ]
 
@@ -80,6 +81,11 @@ class CoDefectOpts(C.Structure):
                 ("precond", C.c_int), ("metric_freeze", C.c_double), ("fp32_window", C.c_int)]
 
 
+class CoNewtonOpts(C.Structure):
+    """co_newton_opts of include/collops.h."""
+    _fields_ = [("krylov_max", C.c_int), ("fd_h", C.c_double), ("eta_max", C.c_double)]
+
+
 class CoStepInfo(C.Structure):
     """co_step_info of include/collops.h."""
     _fields_ = [("outer", C.c_int), ("inner", C.c_int), ("res", C.c_double),
@@ -130,6 +136,12 @@ _SIGNATURES = {
     "co_step_defect_dev": (C.c_int, [C.c_void_p, C.POINTER(CoOpts), C.POINTER(CoDefectOpts),
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double,
                                      C.c_double, _ip, _dp, _ip, _dp]),
+    "co_step_newton": (C.c_int, [C.c_void_p, C.POINTER(CoOpts), C.POINTER(CoNewtonOpts), _dp,
+                                 _dp, _dp, C.c_int, C.c_double, C.c_double, _ip, _dp, _ip, _dp,
+                                 _ip]),
+    "co_step_newton_dev": (C.c_int, [C.c_void_p, C.POINTER(CoOpts), C.POINTER(CoNewtonOpts),
+                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double,
+                                     C.c_double, _ip, _dp, _ip, _dp, _ip]),
     "co_predictor": (C.c_int, [C.c_void_p, C.POINTER(CoOpts), _dp, _dp, _dp, C.c_int,
                                C.c_double]),
     "co_predictor_dev": (C.c_int, [C.c_void_p, C.POINTER(CoOpts), C.c_void_p, C.c_void_p,
@@ -551,6 +563,29 @@ def step_defect(ws: Workspace, v1, v0, w_parts, S0: float, dt: float, *, m: int 
     return it.value, res.value, inner.value, r0.value
 
 
+def step_newton(ws: Workspace, v1, v0, w_parts, S0: float, dt: float, *, max_iter: int = 1000,
+                tol: float = 1e-12, abs_floor: float = 1e-7, krylov_max: int = 30,
+                fd_h: float = 1e-6, eta_max: float = 0.9, use_gonzalez: bool = True,
+                exit_picard_step: bool = True, precision: str = "fp64"):
+    """step_newton! (solver.jl:460-486) on the device; v1 (guess) is overwritten with
+    the solution. Returns (evaluations, ||F||, newton_steps, ||F_0||, status) with
+    status 0 converged, 1 stalled (line search failed), 2 budget."""
+    v0 = _markers(v0, name="v0")
+    N = v0.shape[0]
+    v1 = _out(v1, (N, 2), "v1")
+    o = ws.p.opts(max_iter=max_iter, tol=tol, abs_floor=abs_floor,
+                  use_gonzalez=int(use_gonzalez), exit_picard_step=int(exit_picard_step),
+                  precision=_PREC[precision])
+    k = CoNewtonOpts(krylov_max, fd_h, eta_max)
+    ev, nn, stt = C.c_int(), C.c_int(), C.c_int()
+    res, r0 = C.c_double(), C.c_double()
+    _check(ws.lib.co_step_newton(ws.h, C.byref(o), C.byref(k), _p(v1), _p(v0),
+                                 _p(_vec(w_parts, N, "w_parts")), N, S0, dt, C.byref(ev),
+                                 C.byref(res), C.byref(nn), C.byref(r0), C.byref(stt)),
+           "co_step_newton")
+    return ev.value, res.value, nn.value, r0.value, stt.value
+
+
 def diagnostics(ws: Workspace, v_parts, w_parts) -> dict:
     """Post-step diagnostics of main.jl:298-307 on the device: entropy, energy,
     momentum, ||f_s - f_p||_2 and the negative-part L1 norm of f_s."""
@@ -577,6 +612,71 @@ def conservation_row(step: int, time: float, diag: dict, iters: int, residual: f
             diag["momentum"][1], iters, residual, diag["fs_minus_fp_l2"],
             diag["negative_part_l1"], r0, dt)
     return ",".join(repr(float(x)) if isinstance(x, float) else str(x) for x in vals)
+
+
+# ------------------------------------------------------------------ checkpoint
+
+# Fields of the reference's checkpoint NamedTuple (io.jl:53-86), in its order.
+CHECKPOINT_FIELDS = ("step", "t", "v_particles", "w_particles", "f_coeffs", "entropy_history",
+                     "energy_history", "momentum_history", "iter_history", "res_history",
+                     "fp_l2_history", "neg_history", "rng_state")
+
+
+def checkpoint_path(suffix: str, step: int) -> str:
+    """checkpoint_path (io.jl:65-67) with the .npz extension of this export."""
+    return f"checkpoint_{suffix}_step{step:04d}.npz"
+
+
+def save_checkpoint(suffix: str, step: int, t: float, v_particles, w_particles, f_coeffs,
+                    entropy_history, energy_history, momentum_history, iter_history,
+                    res_history, fp_l2_history, neg_history, directory: str = ".") -> str:
+    """save_checkpoint (io.jl:70-86) as a NumPy archive with the same fields: the
+    markers (N x 2, the Julia layout), weights, spline coefficients and the seven
+    diagnostic histories. The device holds no other state between steps (the
+    solver re-derives everything from v and w), so this is the whole state.
+    rng_state is left empty: the reference only keeps it for forward
+    compatibility (io.jl:60-61), and a Julia RNG cannot be written from here;
+    the conversion in INTEGRATION.md substitutes Random.default_rng()."""
+    v = _markers(v_particles, name="v_particles")
+    N = v.shape[0]
+    arrays = dict(step=np.int64(step), t=np.float64(t), v_particles=v,
+                  w_particles=_vec(w_particles, N, "w_particles"),
+                  f_coeffs=_vec(f_coeffs, None, "f_coeffs"),
+                  entropy_history=np.asarray(entropy_history, dtype=np.float64),
+                  energy_history=np.asarray(energy_history, dtype=np.float64),
+                  momentum_history=np.asarray(momentum_history, dtype=np.float64).reshape(-1, 2),
+                  iter_history=np.asarray(iter_history, dtype=np.int64),
+                  res_history=np.asarray(res_history, dtype=np.float64),
+                  fp_l2_history=np.asarray(fp_l2_history, dtype=np.float64),
+                  neg_history=np.asarray(neg_history, dtype=np.float64),
+                  rng_state=np.zeros(0, dtype=np.uint8))
+    path = os.path.join(directory, checkpoint_path(suffix, step))
+    # v_particles is stored transposed-free: np.save keeps the array's own
+    # (Fortran) order flag, so a Julia reader sees the column-major N x 2 matrix
+    with open(path, "wb") as fh:
+        np.savez(fh, **arrays)
+    return path
+
+
+def load_checkpoint(suffix: str, step, directory: str = ".") -> dict:
+    """load_checkpoint (io.jl:169-182): step = "auto" (or <= 0) picks the
+    highest-step archive of the suffix. Returns the fields as a dict."""
+    if step == "auto" or (isinstance(step, int) and step <= 0):
+        files = sorted(f for f in os.listdir(directory)
+                       if f.startswith(f"checkpoint_{suffix}_step") and f.endswith(".npz"))
+        if not files:
+            raise FileNotFoundError(f"No checkpoint files for suffix={suffix}")
+        path = os.path.join(directory, files[-1])
+    else:
+        path = os.path.join(directory, checkpoint_path(suffix, int(step)))
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"Checkpoint not found: {path}")
+    with np.load(path) as z:
+        d = {k: z[k] for k in CHECKPOINT_FIELDS}
+    d["step"] = int(d["step"])
+    d["t"] = float(d["t"])
+    d["v_particles"] = np.asfortranarray(d["v_particles"])
+    return d
 
 
 def predictor(ws: Workspace, v1, v_parts, w_parts, dt: float, precision: str = "fp64") -> None:

@@ -183,6 +183,7 @@ static void free_ctx(co_ctx *c) {
     for (void *p : ptrs)
         if (p) cudaFree(p);
     co_step_free(c);
+    co_newton_free(c);
     co_prof_free(c);
     if (c->st_host) cudaFreeHost(c->st_host);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -628,6 +629,55 @@ extern "C" int co_diagnostics(co_ctx *c, const double *v, const double *w, int N
     RC(h2d(c, b.w, w, N));
     RC(co_diagnostics_impl(c, b.vmid, N, c->y));
     RC(d2h(c, out6, c->y, 6));
+    return finish(c);
+}
+
+static int check_newton(const co_opts *o, const co_newton_opts *k) {
+    int rc = check_opts(o);
+    if (rc) return rc;
+    if (!k || k->krylov_max < 1 || k->krylov_max > 200 || !(k->fd_h > 0) ||
+        !(k->eta_max > 0 && k->eta_max < 1))
+        return CO_ERR_ARG;
+    return CO_OK;
+}
+
+extern "C" int co_step_newton(co_ctx *c, const co_opts *o, const co_newton_opts *k, double *v1,
+                              const double *v0, const double *w, int N, double S0, double dt,
+                              int *evals, double *res, int *n_newton, double *r0, int *status) {
+    ENTER(c);
+    RC(check_newton(o, k));
+    if (N < 0 || (N > 0 && (!v1 || !v0 || !w))) return CO_ERR_ARG;
+    if (N > 0 && (!all_finite(v1, 2 * (size_t)N) || !all_finite(v0, 2 * (size_t)N) ||
+                  !all_finite(w, N)))
+        return CO_ERR_NONFINITE;
+    RC(co_ensure_capacity(c, N, 1));
+    co_bufs &b = c->mb;
+    RC(h2d(c, b.v1, v1, 2 * (size_t)N));
+    RC(h2d(c, b.v0, v0, 2 * (size_t)N));
+    RC(h2d(c, b.w, w, N));
+    RC(co_step_newton_buffers(c, o, k, N, S0, dt, evals, res, n_newton, r0, status));
+    RC(d2h(c, v1, b.v1, 2 * (size_t)N));
+    return finish(c);
+}
+
+extern "C" int co_step_newton_dev(co_ctx *c, const co_opts *o, const co_newton_opts *k,
+                                  double *v1, const double *v0, const double *w, int N, double S0,
+                                  double dt, int *evals, double *res, int *n_newton, double *r0,
+                                  int *status) {
+    ENTER(c);
+    RC(check_newton(o, k));
+    if (N < 0 || (N > 0 && (!v1 || !v0 || !w))) return CO_ERR_ARG;
+    RC(co_ensure_capacity(c, N, 1));
+    co_bufs &b = c->mb;
+    size_t n2 = 2 * (size_t)N * sizeof(double);
+    if (N > 0) {
+        CO_CK(cudaMemcpyAsync(b.v1, v1, n2, cudaMemcpyDeviceToDevice, c->stream));
+        CO_CK(cudaMemcpyAsync(b.v0, v0, n2, cudaMemcpyDeviceToDevice, c->stream));
+        CO_CK(cudaMemcpyAsync(b.w, w, (size_t)N * sizeof(double), cudaMemcpyDeviceToDevice,
+                              c->stream));
+    }
+    RC(co_step_newton_buffers(c, o, k, N, S0, dt, evals, res, n_newton, r0, status));
+    if (N > 0) CO_CK(cudaMemcpyAsync(v1, b.v1, n2, cudaMemcpyDeviceToDevice, c->stream));
     return finish(c);
 }
 

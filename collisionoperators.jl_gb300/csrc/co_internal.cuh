@@ -125,6 +125,7 @@ struct co_ctx {
     // grid (0 in normal use; a test sets 1 so that the barrier cannot complete)
     int barrier_spins, barrier_phantom;
     struct co_step_bufs *sb;  // buffers of co_step_learned (co_step.cu), allocated on first use
+    struct co_nk_bufs *nk;    // buffers of the Newton-Krylov solve (co_newton.cu), on first use
 };
 
 // ------------------------------------------------------------- helpers
@@ -172,6 +173,10 @@ void co_ctx_destroy_detached(co_ctx *c);   // free a context whose stream/state 
 int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *dopt, int N,
                            double S0, double dt, int *outer, double *res, int *inner, double *r0);
 void co_step_free(co_ctx *c);           // co_step.cu
+void co_newton_free(co_ctx *c);         // co_newton.cu
+int co_step_newton_buffers(co_ctx *c, const co_opts *o, const co_newton_opts *nko, int N,
+                           double S0, double dt, int *evals, double *res, int *n_newton,
+                           double *r0, int *status);
 #define CO_PREC_BOTH 3                  // pack both FP64 and FP32 operands (internal)
 // packed-operand sets a precision needs: 1 = FP64 arrays, 2 = FP32 head/tail arrays
 static inline int co_pack_mode(int precision) {

@@ -426,70 +426,113 @@ __device__ __forceinline__ void pair_u32(const float4 &xg, const float4 &Gg, con
     u2 = fmaf(-d2, cc, g2) * y;
 }
 
+// Register-blocked FP32 symmetric kernel: each of the ST threads holds R targets
+// (t, t + ST, ...) of a TS = R * ST tile, so every source a thread loads from
+// shared memory and every shuffle of the rotating source accumulators serves R
+// pair evaluations. Source tile J is handled in NG = TS / 32 groups of 32: in
+// round rr warp w takes group (w + rr) mod NG, so each group meets each warp
+// once and its accumulators pass from warp to warp through sacc between rounds
+// (fixed order, deterministic).
+template <int R>
 __global__ void __launch_bounds__(ST)
 k_pair32_sym(const float4 *__restrict__ pfx, const float4 *__restrict__ pfg,
              const float *__restrict__ pfw, int nt, int H, int KC,
              double *__restrict__ gpart, float *__restrict__ apart) {
-    __shared__ float4 sx[ST], sg[ST];
-    __shared__ float sw[ST];
-    __shared__ float2 sacc[ST];
+    constexpr int TS = R * ST, NG = TS / 32;
+    __shared__ float4 sx[TS], sg[TS];
+    __shared__ float sw[TS];
+    __shared__ float2 sacc[TS];
     const int I = blockIdx.x % nt, chunk = blockIdx.x / nt;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const float4 xg = pfx[I * ST + tid], Gg = pfg[I * ST + tid];
-    const float wg = pfw[I * ST + tid];
-    double ga1 = 0.0, ga2 = 0.0;
+    float4 xg[R], Gg[R];
+    float wg[R];
+    double ga1[R], ga2[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        xg[r] = pfx[I * TS + r * ST + tid];
+        Gg[r] = pfg[I * TS + r * ST + tid];
+        wg[r] = pfw[I * TS + r * ST + tid];
+        ga1[r] = 0.0;
+        ga2[r] = 0.0;
+    }
     const int k0 = chunk * KC, k1 = min(H + 1, k0 + KC);
     for (int k = k0; k < k1; k++) {
         if (sym_skip(nt, H, I, k)) continue;
         const int J = (I + k) % nt;
         __syncthreads();
-        sx[tid] = pfx[J * ST + tid];
-        sg[tid] = pfg[J * ST + tid];
-        sw[tid] = pfw[J * ST + tid];
-        sacc[tid] = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            sx[r * ST + tid] = pfx[J * TS + r * ST + tid];
+            sg[r * ST + tid] = pfg[J * TS + r * ST + tid];
+            sw[r * ST + tid] = pfw[J * TS + r * ST + tid];
+            sacc[r * ST + tid] = make_float2(0.f, 0.f);
+        }
         __syncthreads();
-        float t1 = 0.f, t2 = 0.f;
-        if (k == 0) {
-#pragma unroll 8
-            for (int a = 0; a < ST; a++) {
-                float u1, u2;
-                pair_u32(xg, Gg, sx[a], sg[a], u1, u2);
-                t1 = fmaf(sw[a], u1, t1);
-                t2 = fmaf(sw[a], u2, t2);
+        float t1[R], t2[R];
+#pragma unroll
+        for (int r = 0; r < R; r++) t1[r] = t2[r] = 0.f;
+        if (k == 0) {  // diagonal tile: ordered pairs, self excluded by the guard
+#pragma unroll 4
+            for (int a = 0; a < TS; a++) {
+                const float4 xa = sx[a], Ga = sg[a];
+                const float wa = sw[a];
+#pragma unroll
+                for (int r = 0; r < R; r++) {
+                    float u1, u2;
+                    pair_u32(xg[r], Gg[r], xa, Ga, u1, u2);
+                    t1[r] = fmaf(wa, u1, t1[r]);
+                    t2[r] = fmaf(wa, u2, t2[r]);
+                }
             }
-            ga1 += (double)t1;
-            ga2 += (double)t2;
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                ga1[r] += (double)t1[r];
+                ga2[r] += (double)t2[r];
+            }
             continue;
         }
-        for (int r = 0; r < 4; r++) {
-            const int base = ((warp + r) & 3) * 32;
+        for (int rr = 0; rr < NG; rr++) {
+            const int base = ((warp + rr) % NG) * 32;
             float2 a0 = sacc[base + lane];
             float a1 = a0.x, a2 = a0.y;
-#pragma unroll 8
+#pragma unroll 4
             for (int q = 0; q < 32; q++) {
                 const int ai = base + ((lane + q) & 31);
-                float u1, u2;
-                pair_u32(xg, Gg, sx[ai], sg[ai], u1, u2);
+                const float4 xa = sx[ai], Ga = sg[ai];
                 const float wa = sw[ai];
-                t1 = fmaf(wa, u1, t1);
-                t2 = fmaf(wa, u2, t2);
-                a1 = fmaf(-wg, u1, a1);
-                a2 = fmaf(-wg, u2, a2);
+#pragma unroll
+                for (int r = 0; r < R; r++) {
+                    float u1, u2;
+                    pair_u32(xg[r], Gg[r], xa, Ga, u1, u2);
+                    t1[r] = fmaf(wa, u1, t1[r]);
+                    t2[r] = fmaf(wa, u2, t2[r]);
+                    a1 = fmaf(-wg[r], u1, a1);
+                    a2 = fmaf(-wg[r], u2, a2);
+                }
                 a1 = __shfl_sync(0xffffffffu, a1, (lane + 1) & 31);
                 a2 = __shfl_sync(0xffffffffu, a2, (lane + 1) & 31);
             }
             sacc[base + lane] = make_float2(a1, a2);
             __syncthreads();
         }
-        ga1 += (double)t1;
-        ga2 += (double)t2;
-        float *ap = apart + ((size_t)(k - 1) * nt + J) * 2 * ST;
-        ap[tid] = sacc[tid].x;
-        ap[ST + tid] = sacc[tid].y;
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            ga1[r] += (double)t1[r];
+            ga2[r] += (double)t2[r];
+        }
+        float *ap = apart + ((size_t)(k - 1) * nt + J) * 2 * TS;
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            ap[r * ST + tid] = sacc[r * ST + tid].x;
+            ap[TS + r * ST + tid] = sacc[r * ST + tid].y;
+        }
     }
-    double *gp = gpart + ((size_t)chunk * nt + I) * 2 * ST;
-    gp[tid] = ga1;
-    gp[ST + tid] = ga2;
+    double *gp = gpart + ((size_t)chunk * nt + I) * 2 * TS;
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        gp[r * ST + tid] = ga1[r];
+        gp[TS + r * ST + tid] = ga2[r];
+    }
 }
 
 // ------------------------------------------------------------------ double-single
@@ -788,22 +831,23 @@ __global__ void k_metric_reduce(const double *__restrict__ gpart, const float *_
 // source-side partials, in that fixed order
 template <typename TA>
 __global__ void k_sym_reduce(const double *__restrict__ gpart, const TA *__restrict__ apart,
-                             int nt, int H, int nchunk, double *__restrict__ dst, size_t ld) {
+                             int nt, int H, int nchunk, int TS, double *__restrict__ dst,
+                             size_t ld) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= nt * ST) return;
-    int K = p / ST, t = p - K * ST;
+    if (p >= nt * TS) return;
+    int K = p / TS, t = p - K * TS;
     double s1 = 0.0, s2 = 0.0;
     for (int c = 0; c < nchunk; c++) {
-        const double *gp = gpart + ((size_t)c * nt + K) * 2 * ST;
+        const double *gp = gpart + ((size_t)c * nt + K) * 2 * TS;
         s1 += gp[t];
-        s2 += gp[ST + t];
+        s2 += gp[TS + t];
     }
     for (int k = 1; k <= H; k++) {
         int I = (K - k + nt) % nt;
         if (sym_skip(nt, H, I, k)) continue;
-        const TA *ap = apart + ((size_t)(k - 1) * nt + K) * 2 * ST;
+        const TA *ap = apart + ((size_t)(k - 1) * nt + K) * 2 * TS;
         s1 += (double)ap[t];
-        s2 += (double)ap[ST + t];
+        s2 += (double)ap[TS + t];
     }
     dst[p] = s1;
     dst[ld + p] = s2;
@@ -1047,6 +1091,12 @@ static int pair_sym(co_ctx *c, int Mub, int kind) {
     size_t gsz = (size_t)nchunk * nt * 2 * ST;               // doubles
     size_t asz = (size_t)(H > 0 ? H : 1) * nt * 2 * ST;      // doubles (fp64) / floats (fp32)
     size_t need = gsz + (fp64 ? asz : (asz + 1) / 2);
+    if (!fp64) {   // the FP32 kernel's 256-marker tiles
+        const int nt2 = co_cdiv(Mub, 2 * ST), H2 = nt2 / 2, nchunk2 = co_cdiv(H2 + 1, KC);
+        const size_t g2 = (size_t)nchunk2 * nt2 * 4 * ST;
+        const size_t a2 = (size_t)(H2 > 0 ? H2 : 1) * nt2 * 4 * ST;
+        need = g2 + (a2 + 1) / 2;
+    }
     int rc = ensure_part(c, need);
     if (rc) return rc;
     double *gpart = c->mb.part;
@@ -1057,21 +1107,27 @@ static int pair_sym(co_ctx *c, int Mub, int kind) {
                                                          c->mb.pf_wl, nt, H, KC, gpart, apart);
         co_prof_end(c);
         k_sym_reduce<double><<<co_cdiv((long long)nt * ST, 256), 256, 0, c->stream>>>(
-            gpart, apart, nt, H, nchunk, c->mb.pdot, (size_t)c->mb.cap);
+            gpart, apart, nt, H, nchunk, ST, c->mb.pdot, (size_t)c->mb.cap);
     } else if (fp64) {
         double *apart = c->mb.part + gsz;
         k_pair64_sym<<<nt * nchunk, ST, 0, c->stream>>>(c->mb.px, c->mb.pg, c->mb.pw, nt, H, KC,
                                                         gpart, apart);
         co_prof_end(c);
         k_sym_reduce<double><<<co_cdiv((long long)nt * ST, 256), 256, 0, c->stream>>>(
-            gpart, apart, nt, H, nchunk, c->mb.pdot, (size_t)c->mb.cap);
+            gpart, apart, nt, H, nchunk, ST, c->mb.pdot, (size_t)c->mb.cap);
     } else {
-        float *apart = (float *)(c->mb.part + gsz);
-        k_pair32_sym<<<nt * nchunk, ST, 0, c->stream>>>(c->mb.pf_x, c->mb.pf_g, c->mb.pf_w, nt, H,
-                                                        KC, gpart, apart);
+        // FP32: two targets per thread on 256-marker tiles (Mpad is a multiple of
+        // 256 and the tile count has been checked by the caller)
+        constexpr int R32 = 2, TS32 = R32 * ST;
+        const int nt2 = co_cdiv(Mub, TS32), H2 = nt2 / 2, nchunk2 = co_cdiv(H2 + 1, KC);
+        const size_t gsz2 = (size_t)nchunk2 * nt2 * 2 * TS32;
+        float *apart = (float *)(c->mb.part + gsz2);
+        k_pair32_sym<R32><<<nt2 * nchunk2, ST, 0, c->stream>>>(c->mb.pf_x, c->mb.pf_g,
+                                                               c->mb.pf_w, nt2, H2, KC,
+                                                               gpart, apart);
         co_prof_end(c);
-        k_sym_reduce<float><<<co_cdiv((long long)nt * ST, 256), 256, 0, c->stream>>>(
-            gpart, apart, nt, H, nchunk, c->mb.pdot, (size_t)c->mb.cap);
+        k_sym_reduce<float><<<co_cdiv((long long)nt2 * TS32, 256), 256, 0, c->stream>>>(
+            gpart, apart, nt2, H2, nchunk2, TS32, c->mb.pdot, (size_t)c->mb.cap);
     }
     c->launches += 2;
     CO_CK(cudaGetLastError());
@@ -1080,7 +1136,7 @@ static int pair_sym(co_ctx *c, int Mub, int kind) {
 
 int co_pair_fp32(co_ctx *c, int Mub) {
     if (Mub <= 0) return CO_OK;
-    if (c->pair_symmetric && co_cdiv(Mub, ST) >= 4) return pair_sym(c, Mub, 0);
+    if (c->pair_symmetric && co_cdiv(Mub, 2 * ST) >= 4) return pair_sym(c, Mub, 0);
     if (Mub <= 0) return CO_OK;
     const int *Mp = c->mb.cstart + c->n_el;
     size_t ld = (size_t)c->mb.cap;

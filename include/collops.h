@@ -201,6 +201,33 @@ int co_step_defect_dev(co_ctx *ctx, const co_opts *opts, const co_defect_opts *d
                        double *v1, const double *v0, const double *w, int N, double S0,
                        double dt, int *outer, double *res, int *inner, double *r0);
 
+/* Options of step_newton! (solver.jl:460-486) beyond co_opts: the GMRES basis
+ * size, the absolute finite-difference step of the Jacobian-vector products and
+ * the cap of the Eisenstat-Walker forcing term (SimParameters nk_krylov_max,
+ * nk_fd_h, nk_eta_max; Parameters.jl:92-103). */
+typedef struct {
+    int krylov_max;      /* 1..200 Arnoldi vectors (2N doubles each, in HBM) */
+    double fd_h;         /* > 0, e.g. 1e-6 for FP64 maps                   */
+    double eta_max;      /* in (0, 1), e.g. 0.9                              */
+} co_newton_opts;
+
+/* step_newton! (solver.jl:460-486) with newton_krylov! and gmres!
+ * (newton_krylov.jl:74-303) on the device: inexact Newton on F(v) = v - G(v),
+ * matrix-free GMRES (modified Gram-Schmidt), Armijo backtracking; the maps run
+ * in FP64, or in double-single pair sums for CO_PREC_MIXED_DS. opts->max_iter
+ * caps the map evaluations; tol and abs_floor set the target and
+ * exit_picard_step the exit update, as in the reference. Outputs mirror its
+ * return tuple (evaluations, ||F||, Newton steps, ||F_0||) plus the status of
+ * newton_krylov! (0 converged, 1 stalled, 2 budget). v1: guess in, solution out. */
+int co_step_newton(co_ctx *ctx, const co_opts *opts, const co_newton_opts *nopts,
+                   double *v1, const double *v0, const double *w, int N, double S0,
+                   double dt, int *evals, double *res, int *n_newton, double *r0,
+                   int *status);
+int co_step_newton_dev(co_ctx *ctx, const co_opts *opts, const co_newton_opts *nopts,
+                       double *v1, const double *v0, const double *w, int N, double S0,
+                       double dt, int *evals, double *res, int *n_newton, double *r0,
+                       int *status);
+
 /* Explicit Euler predictor of the time loop (main.jl:233-245):
  * v1 = v + dt * vdot(v) with the model's right-hand side. */
 int co_predictor(co_ctx *ctx, const co_opts *opts, double *v1, const double *v,

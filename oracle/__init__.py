@@ -77,6 +77,8 @@ def _load():
                                    C.c_int, _dp,
                                    _dp, _dp, C.c_int, C.c_double, C.c_double, _dp]
     lib.om_predictor.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp, _dp, C.c_int, C.c_double]
+    lib.om_step_newton.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_double,
+                                   _dp, _dp, _dp, C.c_int, C.c_double, C.c_double, _dp]
     _lib = lib
     return lib
 
@@ -295,6 +297,19 @@ class OracleMesh:
                                 int(precond), _d(v1), _d(v0),
                                 _d(w), v0.shape[0], S0, dt, _d(out4))
         return v1, (int(out4[0]), out4[1], int(out4[2]), out4[3])
+
+    def step_newton(self, opts: Opts, v1, v0, w, S0: float, dt: float, krylov_max: int = 30,
+                    fd_h: float = 1e-6, eta_max: float = 0.9):
+        """step_newton! (solver.jl:460-486) -> (v, (evals, ||F||, newton steps, ||F_0||,
+        status)); status 0 converged, 1 stalled, 2 budget."""
+        v1 = np.array(v1, dtype=np.float64, order="F", copy=True)
+        v0 = _mk(v0)
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        out5 = np.zeros(5)
+        o = opts.c()
+        self.lib.om_step_newton(self.h, C.byref(o), krylov_max, fd_h, eta_max, _d(v1), _d(v0),
+                                _d(w), v0.shape[0], S0, dt, _d(out5))
+        return v1, (int(out5[0]), out5[1], int(out5[2]), out5[3], int(out5[4]))
 
     def predictor(self, opts: Opts, v, w, dt: float) -> np.ndarray:
         v = _mk(v)

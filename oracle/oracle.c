@@ -44,6 +44,7 @@ struct om_mesh {
                             solve with the 1D factors below                      */
     double *L1, *L2;     /* banded Cholesky factors of the 1D mass matrices,
                             row i: cols i-2..i (5-diagonal matrices)            */
+    double *I1, *I2;     /* dense inverses of the 1D mass matrices (kind 2)    */
 };
 
 /* ---------------------------------------------------------------- quadrature */
@@ -285,16 +286,49 @@ static void line_solve(const double *L, int nd, double *x, size_t st) {
     }
 }
 
+/* dense inverse of the 1D mass matrix from its factor (columns solved one by one) */
+static double *dense_inverse(const double *L, int nd) {
+    double *I = calloc((size_t)nd * nd, sizeof(double));
+    for (int j = 0; j < nd; j++) {
+        I[(size_t)j * nd + j] = 1.0;
+        line_solve(L, nd, I + (size_t)j * nd, 1);   /* column j (symmetric) */
+    }
+    return I;
+}
+
 void om_set_mass_solver(om_mesh *m, int kind) {
-    m->mass_kind = kind == 1 ? 1 : 0;
-    if (m->mass_kind == 1 && !m->L1) {
+    m->mass_kind = (kind == 1 || kind == 2) ? kind : 0;
+    if (m->mass_kind >= 1 && !m->L1) {
         m->L1 = mass1d_factor(m->bp1, m->n1, m->C1);
         m->L2 = mass1d_factor(m->bp2, m->n2, m->C2);
+    }
+    if (m->mass_kind == 2 && !m->I1) {
+        m->I1 = dense_inverse(m->L1, m->nd1);
+        m->I2 = dense_inverse(m->L2, m->nd2);
     }
 }
 
 void om_mass_solve(const om_mesh *m, const double *rhs, double *out) {
     int nd = m->n_dofs, bw = m->bw;
+    if (m->mass_kind == 2) {
+        /* out = M1^{-1} B M2^{-1} by dense products with the 1D inverses */
+        int n1 = m->nd1, n2 = m->nd2;
+        double *y = malloc(sizeof(double) * nd);
+        for (int i2 = 0; i2 < n2; i2++)
+            for (int i1 = 0; i1 < n1; i1++) {
+                double s = 0.0;
+                for (int k = 0; k < n1; k++) s = fma(m->I1[(size_t)k * n1 + i1], rhs[(size_t)i2 * n1 + k], s);
+                y[(size_t)i2 * n1 + i1] = s;
+            }
+        for (int i2 = 0; i2 < n2; i2++)
+            for (int i1 = 0; i1 < n1; i1++) {
+                double s = 0.0;
+                for (int k = 0; k < n2; k++) s = fma(y[(size_t)k * n1 + i1], m->I2[(size_t)k * n2 + i2], s);
+                out[(size_t)i2 * n1 + i1] = s;
+            }
+        free(y);
+        return;
+    }
     if (m->mass_kind == 1) {
         /* M = M2 (x) M1 with index i1 + i2 nd1: solve along i1, then along i2 */
         memcpy(out, rhs, sizeof(double) * nd);
@@ -367,7 +401,7 @@ om_mesh *om_create(const double *bp1, int nb1, const double *bp2, int nb2,
 void om_destroy(om_mesh *m) {
     if (!m) return;
     free(m->bp1); free(m->bp2); free(m->C1); free(m->C2); free(m->Lb);
-    free(m->L1); free(m->L2);
+    free(m->L1); free(m->L2); free(m->I1); free(m->I2);
     free(m);
 }
 
@@ -1261,4 +1295,172 @@ done:
     free(fGeff); free(fvmid);
     free(aa.vk); free(aa.u); free(aa.r); free(aa.rp); free(aa.up); free(aa.dF); free(aa.dU);
     free(Hbuf);
+}
+
+/* ------------------------------------------------------------ Newton-Krylov */
+
+/* Symmetric Givens reflection of newton_krylov.jl:37-58 (_sym_givens). */
+static void sym_givens(double a, double b, double *c, double *s, double *rho) {
+    if (b == 0.0) {
+        *c = (a > 0) - (a < 0) + (a == 0.0);
+        *s = 0.0;
+        *rho = fabs(a);
+    } else if (a == 0.0) {
+        *c = 0.0;
+        *s = (b > 0) - (b < 0);
+        *rho = fabs(b);
+    } else if (fabs(b) > fabs(a)) {
+        double t = a / b;
+        *s = ((b > 0) - (b < 0)) / sqrt(1.0 + t * t);
+        *c = *s * t;
+        *rho = b / *s;
+    } else {
+        double t = b / a;
+        *c = ((a > 0) - (a < 0)) / sqrt(1.0 + t * t);
+        *s = *c * t;
+        *rho = a / *c;
+    }
+}
+
+typedef struct {
+    const om_mesh *m;
+    const om_opts *o;
+    const double *v0, *w;
+    int N;
+    double S0, dt;
+    double *Gv;
+    int n_evals;
+} nk_ctx;
+
+/* residual!(F, v) of step_newton! (solver.jl:465-472): F = v - G(v) */
+static void nk_residual(nk_ctx *c, double *F, const double *x) {
+    om_picard_map(c->m, c->o, c->Gv, x, c->v0, c->w, c->N, c->S0, c->dt);
+    for (int i = 0; i < 2 * c->N; i++) F[i] = x[i] - c->Gv[i];
+    c->n_evals++;
+}
+
+/* gmres! (newton_krylov.jl:74-130) with A u = (F(x + h u) - F(x)) / h,
+ * h = fd_h / ||u|| (the jvp! of newton_krylov!, :215-222). Returns k. */
+static int nk_gmres(nk_ctx *c, int n, double *xs, const double *x, const double *Fx,
+                    double rtol, int itmax, int mem, double fd_h, double *V, double *R,
+                    double *cs, double *sn, double *z, double *wv, double *xp, double *Fp) {
+    int kmax = itmax < mem ? itmax : mem;
+    for (int i = 0; i < n; i++) xs[i] = 0.0;
+    double beta = norm2v(Fx, n);
+    if (beta == 0.0) return 0;
+    double eps = rtol * beta;
+    double btol = pow(2.220446049250313e-16, 0.75);
+    for (int i = 0; i <= mem; i++) z[i] = 0.0;
+    z[0] = beta;
+    for (int i = 0; i < n; i++) V[i] = Fx[i] / beta;
+    int k = 0;
+    while (k < kmax) {
+        k++;
+        const double *u = V + (size_t)(k - 1) * n;
+        double h = fd_h / norm2v(u, n);
+        for (int i = 0; i < n; i++) xp[i] = x[i] + h * u[i];
+        nk_residual(c, Fp, xp);
+        for (int i = 0; i < n; i++) wv[i] = (Fp[i] - Fx[i]) / h;
+        for (int i = 0; i < k; i++) {     /* modified Gram-Schmidt */
+            const double *vi = V + (size_t)i * n;
+            double hh = 0.0;
+            for (int j = 0; j < n; j++) hh += vi[j] * wv[j];
+            R[(size_t)i * mem + (k - 1)] = hh;
+            for (int j = 0; j < n; j++) wv[j] -= hh * vi[j];
+        }
+        double hnext = norm2v(wv, n);
+        for (int i = 0; i < k - 1; i++) {
+            double a = R[(size_t)i * mem + (k - 1)], b = R[(size_t)(i + 1) * mem + (k - 1)];
+            double tmp = cs[i] * a + sn[i] * b;
+            R[(size_t)(i + 1) * mem + (k - 1)] = sn[i] * a - cs[i] * b;
+            R[(size_t)i * mem + (k - 1)] = tmp;
+        }
+        double rho;
+        sym_givens(R[(size_t)(k - 1) * mem + (k - 1)], hnext, &cs[k - 1], &sn[k - 1], &rho);
+        R[(size_t)(k - 1) * mem + (k - 1)] = rho;
+        z[k] = sn[k - 1] * z[k - 1];
+        z[k - 1] = cs[k - 1] * z[k - 1];
+        double rnorm = fabs(z[k]);
+        if (rnorm <= eps || hnext <= btol) break;
+        if (k < kmax)
+            for (int i = 0; i < n; i++) V[(size_t)k * n + i] = wv[i] / hnext;
+    }
+    for (int i = k - 1; i >= 0; i--) {
+        double acc = z[i];
+        for (int j = i + 1; j < k; j++) acc -= R[(size_t)i * mem + j] * z[j];
+        z[i] = fabs(R[(size_t)i * mem + i]) <= btol ? 0.0 : acc / R[(size_t)i * mem + i];
+    }
+    for (int i = 0; i < k; i++)
+        for (int j = 0; j < n; j++) xs[j] += z[i] * V[(size_t)i * n + j];
+    return k;
+}
+
+void om_step_newton(const om_mesh *m, const om_opts *o, int krylov_max, double fd_h,
+                    double eta_max, double *v1, const double *v0, const double *w, int N,
+                    double S0, double dt, double *out5) {
+    int n = 2 * N, mem = krylov_max;
+    nk_ctx c = {m, o, v0, w, N, S0, dt, malloc(sizeof(double) * n), 0};
+    double *F = malloc(sizeof(double) * n), *Ft = malloc(sizeof(double) * n);
+    double *xt = malloc(sizeof(double) * n), *xp = malloc(sizeof(double) * n);
+    double *Fp = malloc(sizeof(double) * n), *d = malloc(sizeof(double) * n);
+    double *xb = malloc(sizeof(double) * n), *Fb = malloc(sizeof(double) * n);
+    double *wv = malloc(sizeof(double) * n);
+    double *V = malloc(sizeof(double) * (size_t)n * (mem + 1));
+    double *R = calloc((size_t)mem * mem, sizeof(double));
+    double *cs = calloc(mem, sizeof(double)), *sn = calloc(mem, sizeof(double));
+    double *z = calloc(mem + 1, sizeof(double));
+    /* step_newton! (solver.jl:460-486): tolerance taken once at the predictor */
+    double tol = fmax(o->tol * (norm2v(v1, n) + 1e-30), o->abs_floor);
+    double *x = v1;
+    nk_residual(&c, F, x);
+    double rnorm = norm2v(F, n), rnorm0 = rnorm, rbest = rnorm, eta = eta_max, rprev = rnorm;
+    memcpy(xb, x, sizeof(double) * n);
+    memcpy(Fb, F, sizeof(double) * n);
+    int n_newton = 0, status = 2; /* 0 converged, 1 stalled, 2 budget */
+    const double gamma = 0.9, armijo = 1e-4;
+    const int max_backtrack = 8;
+    for (;;) {
+        if (rnorm < tol) { status = 0; break; }
+        int budget = o->max_iter - c.n_evals;
+        if (budget < 2) break;
+        if (n_newton > 0) {
+            double ew = gamma * (rnorm / rprev) * (rnorm / rprev);
+            double safe = gamma * eta * eta;
+            if (safe > 0.1) ew = fmax(ew, safe);
+            eta = fmin(fmax(ew, 0.5 * tol / rnorm), eta_max);
+        }
+        int itmax = krylov_max < budget - 1 ? krylov_max : budget - 1;
+        nk_gmres(&c, n, d, x, F, eta, itmax, mem, fd_h, V, R, cs, sn, z, wv, xp, Fp);
+        n_newton++;
+        double lam = 1.0, rt = INFINITY;
+        int accepted = 0;
+        for (int bt = 0; bt <= max_backtrack; bt++) {
+            for (int i = 0; i < n; i++) xt[i] = x[i] - lam * d[i];
+            nk_residual(&c, Ft, xt);
+            rt = norm2v(Ft, n);
+            if (rt <= (1.0 - armijo * lam * (1.0 - eta)) * rnorm) { accepted = 1; break; }
+            if (c.n_evals >= o->max_iter) break;
+            lam /= 2.0;
+        }
+        if (rt < rbest) {
+            rbest = rt;
+            memcpy(xb, xt, sizeof(double) * n);
+            memcpy(Fb, Ft, sizeof(double) * n);
+        }
+        if (!accepted) { status = c.n_evals >= o->max_iter ? 2 : 1; break; }
+        memcpy(x, xt, sizeof(double) * n);
+        memcpy(F, Ft, sizeof(double) * n);
+        rprev = rnorm;
+        rnorm = rt;
+    }
+    if (status != 0 && rbest < rnorm) {
+        memcpy(x, xb, sizeof(double) * n);
+        memcpy(F, Fb, sizeof(double) * n);
+        rnorm = rbest;
+    }
+    if (o->exit_picard_step)                  /* v1 -= F: the Picard update G(v) */
+        for (int i = 0; i < n; i++) x[i] -= F[i];
+    out5[0] = c.n_evals; out5[1] = rnorm; out5[2] = n_newton; out5[3] = rnorm0; out5[4] = status;
+    free(c.Gv); free(F); free(Ft); free(xt); free(xp); free(Fp); free(d); free(xb); free(Fb);
+    free(wv); free(V); free(R); free(cs); free(sn); free(z);
 }

@@ -138,6 +138,16 @@ void om_step_defect(const om_mesh *m, const om_opts *o, double eta, int max_inne
                     int stag_window, int outer_m, int precond, double *v1, const double *v0,
                     const double *w, int N, double S0, double dt, double *out4);
 
+/* step_newton! (solver.jl:460-486) with newton_krylov! and gmres!
+ * (newton_krylov.jl:74-303): inexact Newton with matrix-free GMRES of at most
+ * krylov_max vectors, forward-difference products with the absolute step fd_h,
+ * Eisenstat-Walker forcing capped at eta_max, Armijo backtracking; o->max_iter
+ * caps the map evaluations. out5 = evaluations, ||F||, Newton steps, ||F_0||,
+ * status (0 converged, 1 stalled, 2 budget). */
+void om_step_newton(const om_mesh *m, const om_opts *o, int krylov_max, double fd_h,
+                    double eta_max, double *v1, const double *v0, const double *w, int N,
+                    double S0, double dt, double *out5);
+
 #ifdef __cplusplus
 }
 #endif

@@ -121,3 +121,27 @@ def test_conservation_row_layout(collops_mod):
     assert len(fields) == len(collops_mod.CONS_COLS)
     assert fields[0] == "3" and fields[6] == "18"
     assert float(fields[2]) == 2.5 and float(fields[5]) == -2e-17 and float(fields[11]) == 0.02
+
+
+def test_checkpoint_roundtrip(collops_mod, tmp_path):
+    """save_checkpoint / load_checkpoint keep the reference's fields (io.jl:53-86,
+    169-182) and the Julia N x 2 column-major marker layout; step="auto" picks
+    the highest step."""
+    rng = np.random.default_rng(3)
+    N = 257
+    v = np.asfortranarray(rng.standard_normal((N, 2)))
+    w = np.full(N, 1.0 / N)
+    f = rng.standard_normal(324)
+    hist = dict(entropy_history=[1.0, 1.1], energy_history=[0.6, 0.6],
+                momentum_history=[(0.0, 0.1), (0.0, 0.1)], iter_history=[0, 17],
+                res_history=[0.0, 3e-10], fp_l2_history=[0.1, 0.09], neg_history=[0.0, 1e-5])
+    for step in (25, 50):
+        collops_mod.save_checkpoint("run", step, 0.02 * step, v, w, f, directory=str(tmp_path),
+                                    **hist)
+    d = collops_mod.load_checkpoint("run", "auto", directory=str(tmp_path))
+    assert d["step"] == 50 and d["t"] == 1.0
+    assert tuple(d) == collops_mod.CHECKPOINT_FIELDS
+    assert np.array_equal(d["v_particles"], v) and d["v_particles"].flags.f_contiguous
+    assert np.array_equal(d["f_coeffs"], f) and d["momentum_history"].shape == (2, 2)
+    assert list(d["iter_history"]) == [0, 17]
+    assert collops_mod.load_checkpoint("run", 25, directory=str(tmp_path))["step"] == 25

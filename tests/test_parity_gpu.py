@@ -200,8 +200,33 @@ def test_picard_map(setup, collops_mod, oracle_mod, model, gonzalez):
     assert np.max(np.abs(out - ref)) / np.max(np.abs(ref)) < tol
 
 
+def lb_predictor_sensitivity(oracle_mod, om, v, w, dt, trials=3):
+    """How far the oracle's LB predictor moves (relative to max|v1|) when the
+    projection coefficients f_s move by one unit round-off of max|f_s| -- the
+    error model of any FP64 scatter and mass solve. g = grad f_s / f_s divides
+    by f_s, so at a marker where f_s undershoots to ~0 this is far above 1e-16."""
+    f = om.l2_project(v, w)
+
+    def pred(fc):
+        g = om.loggrad(v, fc)
+        n, U1, U2, Q = oracle_mod.moments(v, w)
+        A1, A2, B = oracle_mod.drift_multipliers(v, w, g, n, U1, U2, Q)
+        return v + dt * oracle_mod.lb_velocity(v, g, A1, A2, B, 1.0)
+    p0 = pred(f)
+    rng = np.random.default_rng(0)
+    eps = np.finfo(np.float64).eps * np.max(np.abs(f))
+    return max(np.max(np.abs(pred(f + eps * rng.choice([-1.0, 1.0], f.size)) - p0)) /
+               np.max(np.abs(p0)) for _ in range(trials))
+
+
 @pytest.mark.parametrize("model", ["landau", "lb"])
 def test_predictor(setup, collops_mod, oracle_mod, model):
+    """Explicit predictor v1 = v + dt vdot(v) (main.jl:233-245). Landau: 1e-12.
+    LB evaluates g = grad f_s / f_s at the markers themselves, where a Gibbs
+    undershoot of f_s can sit next to a marker: its tolerance is
+    max(1e-12, 8 x the predictor's change under a one-ulp perturbation of f_s),
+    i.e. a scatter-plus-solve round-off budget of 8 ulps of max|f_s| (measured
+    sensitivity 5e-13 at C2, GPU error 1.7e-12)."""
     om, v, w = setup["om"], setup["v"], setup["w"]
     p = collops_mod.SimParameters(bp1=setup["bp"], bp2=setup["bp"], collision_model=model)
     ws = collops_mod.build_workspace(p)
@@ -210,8 +235,11 @@ def test_predictor(setup, collops_mod, oracle_mod, model):
     collops_mod.predictor(ws, v1, v, w, 0.05)
     ws.close()
     ref = om.predictor(o, v, w, 0.05)
-    tol = TOL_LB if model == "lb" else TOL64
-    assert np.max(np.abs(v1 - ref)) / np.max(np.abs(ref)) < tol
+    tol = TOL64
+    if model == "lb":
+        tol = max(TOL64, 8.0 * lb_predictor_sensitivity(oracle_mod, om, v, w, 0.05))
+    err = np.max(np.abs(v1 - ref)) / np.max(np.abs(ref))
+    assert err < tol, (err, tol)
 
 
 @pytest.mark.parametrize("model", ["landau", "lb"])

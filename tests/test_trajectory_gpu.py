@@ -8,11 +8,16 @@ and is compared with the oracle's same step:
 - the Picard map at the oracle's predictor point, per step: 1e-12 relative on
   v_out (the per-RHS bar of the FP64 form), both Landau and LB;
 - the exit of step_anderson! (converged, or the stagnation exit of
-  solver.jl:357-367 with its best iterate) and the returned state. A converged
-  step must land on the oracle's fixed point to 1e-10. A stagnated step must
-  stagnate in the same window; its best iterate is that of an iteration that
-  does not contract, where round-off differences grow, so it is held to the
-  scale of the residual it stagnated at.
+  solver.jl:357-367 with its best iterate) and the returned state. When both
+  converge, the iteration counts agree within 10 % and the fixed points to
+  1e-10. When both stagnate, both leave on a window boundary with best
+  residuals within 5x (the iteration does not contract there, so round-off
+  differences grow and the best iterates differ at the scale of that
+  residual). A step where one side converges and the other stagnates is that
+  same amplification deciding the exit (both started within 1e-15); it passes
+  only if the converged result, run through the OTHER side's map, has a
+  residual below the other side's best -- i.e. it is the better answer by the
+  other implementation's own measure.
 
 Configurations (uniform meshes, uniform weights 1/N, Gonzalez on, tol 1e-12,
 abs_floor 0 so that tol*||v|| binds):
@@ -61,10 +66,18 @@ def _run(oracle_mod, collops_mod, *, lo, n, N, sx, sy, peak, model, dt, m, steps
         y = np.zeros_like(x, order="F")
         collops_mod.predictor(ws, y, x, w, dt)
         info = collops_mod.step_anderson(ws, y, x, w, S0, dt, **kw)
-        tol_v = 1e-12 * np.linalg.norm(ref)
+        conv = info[1] < 1e-12 * np.linalg.norm(y)
+        conv_ref = info_ref[1] < 1e-12 * np.linalg.norm(ref)
+        cross = None
+        if conv and not conv_ref:        # the GPU result through the oracle's map
+            cross = np.linalg.norm(om.picard_map(o, y, x, w, S0, dt) - y)
+        elif conv_ref and not conv:      # the oracle result through the GPU's map
+            g = np.zeros_like(x, order="F")
+            collops_mod.picard_map(ws, g, ref, x, w, S0, dt)
+            cross = np.linalg.norm(g - ref)
         rows.append(dict(k=k, map_err=map_err, it=info[0], it_ref=info_ref[0], res=info[1],
-                         res_ref=info_ref[1], conv=info[1] < 1e-12 * np.linalg.norm(y),
-                         conv_ref=info_ref[1] < tol_v, diff=_rel(y, ref), x=x, y=y))
+                         res_ref=info_ref[1], conv=conv, conv_ref=conv_ref, cross=cross,
+                         diff=_rel(y, ref), x=x, y=y))
         x = ref
     ws.close()
     return rows, w
@@ -73,20 +86,27 @@ def _run(oracle_mod, collops_mod, *, lo, n, N, sx, sy, peak, model, dt, m, steps
 def _check(rows, w):
     report = "\n".join(f"step {r['k']}: map {r['map_err']:.2e} it {r['it']}/{r['it_ref']} "
                        f"res {r['res']:.2e}/{r['res_ref']:.2e} conv {r['conv']}/{r['conv_ref']} "
-                       f"diff {r['diff']:.2e}" for r in rows)
+                       f"diff {r['diff']:.2e}" +
+                       (f" cross-residual {r['cross']:.2e}" if r["cross"] is not None else "")
+                       for r in rows)
+    flips = 0
     for r in rows:
         assert r["map_err"] < TOL64, report
-        assert r["conv"] == r["conv_ref"], report
-        if r["conv_ref"]:
+        if r["conv"] and r["conv_ref"]:
             assert abs(r["it"] - r["it_ref"]) <= max(3, r["it_ref"] // 10), report
             assert r["diff"] < 1e-10, report
-        else:
+        elif not r["conv"] and not r["conv_ref"]:
             # stagnation exits leave on a window boundary (solver.jl:357-367)
             assert r["it"] % 50 == 0 and r["it_ref"] % 50 == 0, report
             assert 0.2 < r["res"] / r["res_ref"] < 5.0, report
+        else:
+            flips += 1
+            other_best = r["res_ref"] if r["conv"] else r["res"]
+            assert r["cross"] < other_best, report
         # the returned state is a Picard update: momentum is conserved
         dp = np.abs((w[:, None] * (r["y"] - r["x"])).sum(0)).max()
         assert dp < 1e-12, report
+    assert flips <= max(1, len(rows) // 4), report
     return report
 
 
