@@ -1315,6 +1315,8 @@ struct co_batch {
     std::vector<double> nu;
     std::vector<size_t> off;          // marker offset of each instance in concatenated arrays
     co_solver_state *st_all;          // device, n states
+    int *d_loop;                      // device: [0] iterations of the current device loop,
+                                      // [1..] the live instances it covers
     co_solver_state *st_host;         // pinned
     co_bwork *d_tab;
     std::vector<co_bwork> tab;
@@ -1424,7 +1426,8 @@ extern "C" int co_batch_create(const co_batch_instance *inst, int n, int n_quad,
     if (cudaMalloc(&B->st_all, sizeof(co_solver_state) * n) != cudaSuccess ||
         cudaMallocHost(&B->st_host, sizeof(co_solver_state) * n) != cudaSuccess ||
         cudaMalloc(&B->d_tab, sizeof(co_bwork) * (n + 1)) != cudaSuccess ||
-        cudaMalloc(&B->d_counter, 64) != cudaSuccess) {
+        cudaMalloc(&B->d_counter, 64) != cudaSuccess ||
+        cudaMalloc(&B->d_loop, sizeof(int) * (n + 1)) != cudaSuccess) {
         co_batch_destroy(B);
         return CO_ERR_NOMEM;
     }
@@ -1481,6 +1484,7 @@ extern "C" int co_batch_destroy(co_batch *B) {
         co_ctx_destroy_detached(c);
     }
     if (B->st_all) cudaFree(B->st_all);
+    if (B->d_loop) cudaFree(B->d_loop);
     if (B->st_host) cudaFreeHost(B->st_host);
     if (B->d_tab) cudaFree(B->d_tab);
     if (B->d_counter) cudaFree(B->d_counter);
@@ -1567,6 +1571,22 @@ static int batch_iteration_impl(co_batch *B, const co_opts *o, const double *S0,
     if ((rc = batch_join(B, B->ev_join2))) return rc;
     CO_CK(cudaGetLastError());
     return CO_OK;
+}
+
+// Condition of the device-side iteration loop of the batch engine: one more
+// iteration while every instance the loop covers is still running and the
+// loop has done fewer than `cap` iterations. The loop ends on the device as
+// soon as any instance finishes, so the host only wakes to shrink the live set.
+__global__ void k_batch_continue(cudaGraphConditionalHandle h, const co_solver_state *st_all,
+                                 int *loop, int nlive, int cap) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int k = ++loop[0];
+    unsigned go = k < cap ? 1u : 0u;
+    for (int j = 0; j < nlive && go; j++) {
+        const co_solver_state &st = st_all[loop[1 + j]];
+        if (st.finished || st.error) go = 0u;
+    }
+    cudaGraphSetConditional(h, go);
 }
 
 static int batch_iteration(co_batch *B, const co_opts *o, const double *S0, double dt,
@@ -1664,33 +1684,61 @@ extern "C" int co_batch_step_dev(co_batch *B, const co_opts *o, double *v1_all,
     } else if ((rc = batch_rebuild_table(B))) {
         return rc;
     }
-    // the iteration of the live instances as a CUDA graph, re-captured whenever
-    // the live set shrinks (finished instances then cost nothing per iteration)
+    // The iteration of the live instances as a CUDA graph whose body repeats on
+    // the device (a conditional WHILE node; k_batch_continue decides) until an
+    // instance finishes or the cap is reached. The host then reads the states
+    // once, drops finished instances from the live set and re-captures, so
+    // finished instances cost nothing per iteration and the host waits once per
+    // change of the live set, not once per iteration.
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;
-    auto capture = [&]() -> int {
+    auto capture = [&](int cap) -> int {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
         exec = nullptr;
         graph = nullptr;
         CO_CK(cudaStreamSynchronize(B->stream));
-        CO_CK(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
+        std::vector<int> hl(1 + B->live.size(), 0);
+        for (size_t j = 0; j < B->live.size(); j++) hl[1 + j] = B->live[j];
+        CO_CK(cudaMemcpy(B->d_loop, hl.data(), sizeof(int) * hl.size(), cudaMemcpyHostToDevice));
+        CO_CK(cudaGraphCreate(&graph, 0));
+        cudaGraphConditionalHandle hnd;
+        CO_CK(cudaGraphConditionalHandleCreate(&hnd, graph, 1, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams np = {};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = hnd;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t node;
+        CO_CK(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np));
+        cudaGraph_t body = np.conditional.phGraph_out[0];
+        CO_CK(cudaStreamBeginCaptureToGraph(B->stream, body, nullptr, nullptr, 0,
+                                            cudaStreamCaptureModeThreadLocal));
         int r = batch_iteration(B, o, S0, dt, d);
-        cudaError_t ce = cudaStreamEndCapture(B->stream, &graph);
+        if (!r) {
+            k_batch_continue<<<1, 32, 0, B->stream>>>(hnd, B->st_all, B->d_loop,
+                                                      (int)B->live.size(), cap);
+            if (cudaGetLastError() != cudaSuccess) r = CO_ERR_CUDA;
+        }
+        cudaError_t ce = cudaStreamEndCapture(B->stream, &body);
         if (r) return r;
         if (ce != cudaSuccess) return CO_ERR_CUDA;
         if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) return CO_ERR_CUDA;
         return CO_OK;
     };
-    if (use_graph && (rc = capture())) {
+    if (use_graph && (rc = capture(o->max_iter))) {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
         return rc;
     }
-    int k;
-    for (k = 1; k <= o->max_iter; k++) {
+    int k = 0;           // iterations done
+    while (k < o->max_iter) {
+        int ran = 1;
         if (use_graph) {
-            if (cudaGraphLaunch(exec, B->stream) != cudaSuccess) {
+            if (cudaMemsetAsync(B->d_loop, 0, sizeof(int), B->stream) != cudaSuccess ||
+                cudaGraphLaunch(exec, B->stream) != cudaSuccess ||
+                cudaMemcpyAsync(&ran, B->d_loop, sizeof(int), cudaMemcpyDeviceToHost,
+                                B->stream) != cudaSuccess) {
                 rc = CO_ERR_CUDA;
                 break;
             }
@@ -1703,18 +1751,20 @@ extern "C" int co_batch_step_dev(co_batch *B, const co_opts *o, double *v1_all,
             rc = CO_ERR_CUDA;
             break;
         }
+        k += ran;
         std::vector<int> still;
         for (int i : B->live) {
             if (B->st_host[i].error) rc = B->st_host[i].error;
             if (!B->st_host[i].finished) still.push_back(i);
         }
-        if (rc || still.empty()) break;
+        if (rc || still.empty() || k >= o->max_iter) break;
         if (still.size() < B->live.size()) {
             B->live.swap(still);
             if ((rc = batch_rebuild_table(B))) break;
-            if (use_graph && (rc = capture())) break;
+            if (use_graph && (rc = capture(o->max_iter - k))) break;
         }
     }
+    if (k >= o->max_iter) k = o->max_iter + 1;   // the cap: best iterates below
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     if (rc) return rc;

@@ -83,3 +83,77 @@ def test_batch_tuner_choices(built_lib, collops_mod):
     t = batch.tune()
     batch.close()
     assert t["warps"] in (4, 8) and t["chunk"] in (4, 16) and t["pair_ms"] > 0
+
+
+def test_batch_matches_oracle_with_gonzalez(built_lib, collops_mod, oracle_mod):
+    """Every instance of a batched step (Gonzalez on, dt 0.001, two consecutive
+    steps) against the oracle's step_anderson! on the same state. Landau
+    instances converge and land on the oracle's fixed point to 1e-10 with
+    iteration counts within 10 %. The LB instances mostly stagnate in the
+    reference algorithm too (the Gonzalez-corrected LB map does not contract on
+    these coarse meshes): when both stagnate they leave on a window boundary
+    with best residuals within 5x; when round-off lets one side converge where
+    the other stagnates, the converged state must have a smaller residual on the
+    other side's map than that side's best. Every exit Picard update conserves
+    momentum; energy is conserved at a fixed point, so it is checked on the
+    converged instances."""
+    import torch
+    vs, ws, descs, vcat, wcat = _setup()
+    dt = 0.001
+    p = collops_mod.SimParameters(m_anderson=5, damping=0.7, tol=1e-12, abs_floor=0.0,
+                                  max_iter=400, use_gonzalez=True)
+    o = p.opts()
+    batch = collops_mod.Batch(descs)
+    x = vcat
+    states = [[v] for v in vs]
+    recs = []
+    for _step in range(2):
+        S0 = batch.entropy(x, wcat)
+        v1 = torch.empty_like(x)
+        batch.predictor(o, v1, x, wcat, dt)
+        iters, res = batch.step(o, v1, x, wcat, S0, dt)
+        recs.append((np.array(iters), np.array(res), v1.cpu().numpy()))
+        x = v1
+    batch.close()
+    for k, d in enumerate(descs):
+        N = d["N"]
+        om = oracle_mod.OracleMesh(d["bp1"], d["bp2"], 6)
+        oo = oracle_mod.Opts(model=d["model"], nu=d["nu"], m=5, tol=1e-12, abs_floor=0.0,
+                             damping=0.7, max_iter=400)
+        off = int(sum(dd["N"] for dd in descs[:k]))
+        xk = vs[k]
+        for step, (iters, res, out) in enumerate(recs):
+            got = out[2 * off: 2 * off + 2 * N].reshape(2, N).T
+            S0 = om.entropy(om.l2_project(xk, ws[k]))
+            ref, info = om.step_anderson(oo, om.predictor(oo, xk, ws[k], dt), xk, ws[k], S0, dt)
+            conv = res[k] < 1e-12 * np.linalg.norm(got)
+            conv_ref = info[1] < 1e-12 * np.linalg.norm(ref)
+            msg = (f"instance {k} ({d['model']}, N={N}) step {step}: it {iters[k]}/{info[0]} "
+                   f"res {res[k]:.2e}/{info[1]:.2e}")
+            if d["model"] == "landau":
+                assert conv and conv_ref, msg
+                assert abs(int(iters[k]) - info[0]) <= max(3, info[0] // 10), msg
+                assert np.max(np.abs(got - ref)) / np.max(np.abs(ref)) < 1e-10, msg
+            elif not conv and not conv_ref:
+                assert iters[k] % 50 == 0 and info[0] % 50 == 0, msg
+                assert 0.2 < res[k] / info[1] < 5.0, msg
+            elif conv:
+                # a flip decided by round-off in a non-contracting iteration: the
+                # batch's converged state must beat the oracle's best on the
+                # oracle's own map
+                cross = np.linalg.norm(om.picard_map(oo, got, xk, ws[k], S0, dt) - got)
+                assert cross < info[1], msg + f" cross {cross:.2e}"
+            else:
+                wsk = collops_mod.build_workspace(collops_mod.SimParameters(
+                    bp1=d["bp1"], bp2=d["bp2"], collision_model=d["model"], nu=d["nu"]))
+                g = np.zeros_like(ref, order="F")
+                collops_mod.picard_map(wsk, g, ref, xk, ws[k], S0, dt)
+                wsk.close()
+                cross = np.linalg.norm(g - ref)
+                assert cross < res[k], msg + f" cross {cross:.2e}"
+            w = ws[k]
+            assert np.max(np.abs((w[:, None] * (got - xk)).sum(0))) < 1e-12, msg
+            if conv:
+                E0 = 0.5 * np.sum(w * (xk ** 2).sum(1))
+                assert abs(0.5 * np.sum(w * (got ** 2).sum(1)) - E0) < 1e-12 * E0, msg
+            xk = ref if d["model"] == "landau" else got
