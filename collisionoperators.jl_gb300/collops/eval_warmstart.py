@@ -8,9 +8,9 @@ abs_floor 0; defect correction with the benchmark's settings. Markers are seeded
 
 The same state sequence is advanced `--steps` times; at each step the implicit
 solve is started from
-  - learned:    the network's proposal v_pred + dt^2 * delta (fallback to the
-                predictor when its first residual is larger, so never worse
-                than the predictor at the first iterate);
+  - learned:    the headline rule (co_step_learned, no retry): whichever of
+                the network's proposal v_pred + dt^2 * delta, the predictor and
+                the previous state has the smallest first residual;
   - predictor:  the explicit step v0 + dt * vdot(v0) of main.jl:233-245;
   - previous:   the previous step's state v0 itself;
 and solved to the same tolerance by the same solver. The trajectory follows the
@@ -32,7 +32,8 @@ import numpy as np
 
 WORKLOAD = dict(name="landau_bimodal_n262144_mesh64_dt0.02", N=262144, n_el=64, lo=-8.0,
                 hi=8.0, peak=2.5, T=0.4, dt=0.02, m=8, damping=0.7, tol=1e-12,
-                abs_floor=0.0, max_iter=2000, seed=7)
+                abs_floor=1e-10, max_iter=2000, stag_window=50, stag_rel_tol=0.01,
+                use_logsq=True, seed=7)
 
 
 def bimodal_markers(N: int, peak: float, T: float, seed: int):
@@ -58,7 +59,8 @@ def run(weights: str, steps: int = 3, solver: str = "anderson", form: str = "mix
     bp = np.linspace(cfg["lo"], cfg["hi"], cfg["n_el"] + 1)
     p = co.SimParameters(bp1=bp, bp2=bp, m_anderson=cfg["m"], damping=cfg["damping"],
                          tol=cfg["tol"], abs_floor=cfg["abs_floor"], max_iter=cfg["max_iter"],
-                         precision=form)
+                         stag_window=cfg["stag_window"], stag_rel_tol=cfg["stag_rel_tol"],
+                         use_logsq=cfg["use_logsq"], precision=form)
     ws = co.build_workspace(p, device=device)
     lib, h = ws.lib, ws.h
     stream = torch.cuda.ExternalStream(ws.stream(), device=device)
@@ -70,8 +72,9 @@ def run(weights: str, steps: int = 3, solver: str = "anderson", form: str = "mix
     w = torch.from_numpy(w_np).to(dev)
     v1 = torch.empty_like(x)
     # the benchmark's defect-correction settings: eta 0.02, 100 inner maps, stagnation
-    # window 5, FP32 stage left below a 0.9 cut, outer Anderson depth 5, no inner
-    # preconditioner, FP32 metric frozen after a 1000x residual drop
+    # window 5 (stag_rel_tol from the workload), FP32 stage left below a 0.9 cut,
+    # outer Anderson depth 5, no inner preconditioner, FP32 metric frozen after a
+    # 1000x residual drop
     dopt = co.CoDefectOpts(0.02, 100, 5, 0.9, 0, 5, 0, 1e-3, 0)
 
     def entropy(xx):
@@ -87,31 +90,36 @@ def run(weights: str, steps: int = 3, solver: str = "anderson", form: str = "mix
         torch.cuda.synchronize()
         e0.record(stream)
         used = None
-        if start == "learned":
-            used, _rl, _rp = warm.propose(ws, o, x0, w, S0, dt, v1)
-        elif start == "predictor":
-            co._check(lib.co_predictor_dev(h, C.byref(o), v1.data_ptr(), x0.data_ptr(),
-                                           w.data_ptr(), N, dt), "co_predictor_dev")
-        else:
-            with torch.cuda.stream(stream):
-                v1.copy_(x0)
         it, nrs = C.c_int(), C.c_int()
         res, r0 = C.c_double(), C.c_double()
-        if solver == "defect":
-            o.stag_rel_tol = 0.1
-            co._check(lib.co_step_defect_dev(h, C.byref(o), C.byref(dopt), v1.data_ptr(),
-                                             x0.data_ptr(), w.data_ptr(), N, S0, dt,
-                                             C.byref(it), C.byref(res), C.byref(nrs),
-                                             C.byref(r0)), "co_step_defect_dev")
+        if start == "learned":
+            rec = warm.step(ws, o, dopt if solver == "defect" else None, x0, w, S0, dt, v1,
+                            retry=False)
+            used = rec["start"]
+            it.value, res.value, r0.value = rec["outer"], rec["res"], rec["r0"]
         else:
-            co._check(lib.co_step_anderson_dev(h, C.byref(o), v1.data_ptr(), x0.data_ptr(),
-                                               w.data_ptr(), N, S0, dt, C.byref(it),
-                                               C.byref(res), C.byref(nrs), C.byref(r0)),
-                      "co_step_anderson_dev")
+            if start == "predictor":
+                co._check(lib.co_predictor_dev(h, C.byref(o), v1.data_ptr(), x0.data_ptr(),
+                                               w.data_ptr(), N, dt), "co_predictor_dev")
+            else:
+                with torch.cuda.stream(stream):
+                    v1.copy_(x0)
+            if solver == "defect":
+                co._check(lib.co_step_defect_dev(h, C.byref(o), C.byref(dopt), v1.data_ptr(),
+                                                 x0.data_ptr(), w.data_ptr(), N, S0, dt,
+                                                 C.byref(it), C.byref(res), C.byref(nrs),
+                                                 C.byref(r0)), "co_step_defect_dev")
+            else:
+                co._check(lib.co_step_anderson_dev(h, C.byref(o), v1.data_ptr(), x0.data_ptr(),
+                                                   w.data_ptr(), N, S0, dt, C.byref(it),
+                                                   C.byref(res), C.byref(nrs), C.byref(r0)),
+                          "co_step_anderson_dev")
         e1.record(stream)
         torch.cuda.synchronize()
+        conv = res.value < max(cfg["tol"] * float(torch.linalg.vector_norm(v1)),
+                                cfg["abs_floor"])
         return v1.clone(), dict(iterations=it.value, residual=res.value, first_residual=r0.value,
-                                ms=e0.elapsed_time(e1), learned_used=used)
+                                ms=e0.elapsed_time(e1), start=used, converged=bool(conv))
 
     starts = ("learned", "predictor", "previous")
     rec = {s: [] for s in starts}
@@ -127,10 +135,15 @@ def run(weights: str, steps: int = 3, solver: str = "anderson", form: str = "mix
         S0 = entropy(x)
     summary = {s: dict(iterations_mean=statistics.mean(r["iterations"] for r in rec[s]),
                        ms_per_step=statistics.mean(r["ms"] for r in rec[s]),
+                       converged_steps=sum(r["converged"] for r in rec[s]),
+                       ms_per_converged_step=(statistics.mean(r["ms"] for r in rec[s]
+                                                              if r["converged"])
+                                              if any(r["converged"] for r in rec[s]) else None),
                        residual_max=max(r["residual"] for r in rec[s]),
                        first_residual_mean=statistics.mean(r["first_residual"] for r in rec[s]))
                for s in starts}
-    summary["learned"]["learned_used"] = sum(bool(r["learned_used"]) for r in rec["learned"])
+    summary["learned"]["starts_chosen"] = {k: sum(r["start"] == k for r in rec["learned"])
+                                           for k in ("learned", "predictor", "previous")}
     ws.close()
     return {"workload": cfg["name"], "N": N, "solver": solver, "form": form, "steps": steps,
             "tol": cfg["tol"], "summary": summary, "per_step": rec}

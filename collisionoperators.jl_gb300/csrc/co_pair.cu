@@ -605,17 +605,20 @@ __device__ __forceinline__ void ds_acc(dsf &acc, dsf x) {
     acc.l = __fadd_rn(acc.l, __fadd_rn(x.l, s.l));
 }
 
-// Pair term of the symmetric sum in double-single: with u = U(d)(G_a - G_g)/|d|
-// = y t, y = 1/|d|, t = g - d (d.g) y^2, it returns t (unnormalised) and the
-// weighted inverse distances wy_a = w_a y and wy_g = w_g y (0 for |d|^2 < 1e-24),
-// so that the target gets wy_a t and the source -wy_g t.
-__device__ __forceinline__ void pair_t_ds(const float4 &xg, const float4 &Gg, const float4 &xa,
-                                          const float4 &Ga, dsf wa, dsf wg, dsf &t1, dsf &t2,
-                                          dsf &wya, dsf &wyg) {
+// Pair term of the symmetric sum in double-single. In two dimensions the
+// projection of g = G_a - G_g off d = x_g - x_a is
+//   g - d (d.g)/|d|^2 = c (d2, -d1) / |d|^2,   c = g1 d2 - g2 d1,
+// so u = U(d) g / |d| = s (d2, -d1) with s = c / |d|^3 (the same term as
+// functions.jl:221-231 in exact arithmetic; c carries the cancellation that
+// g - d (d.g)/|d|^2 carries when g is nearly parallel to d). Returns d1, d2 and
+// s (0 for |d|^2 < 1e-24). The target gets w_a s (d2, -d1), the source the
+// same with -w_g.
+__device__ __forceinline__ void pair_s_ds(const float4 &xg, const float4 &Gg, const float4 &xa,
+                                          const float4 &Ga, dsf &d1, dsf &d2, dsf &s) {
     // differences are renormalised: for close markers the heads cancel exactly
     // and the tail difference would otherwise be a large l (the products drop l*l)
-    dsf d1 = ds_norm(ds_add_u({xg.x, xg.z}, {-xa.x, -xa.z}));
-    dsf d2 = ds_norm(ds_add_u({xg.y, xg.w}, {-xa.y, -xa.w}));
+    d1 = ds_norm(ds_add_u({xg.x, xg.z}, {-xa.x, -xa.z}));
+    d2 = ds_norm(ds_add_u({xg.y, xg.w}, {-xa.y, -xa.w}));
     dsf r2 = ds_add_u(ds_sqr_u(d1), ds_sqr_u(d2));
     const bool ok = r2.h >= 1e-24f;
     if (!ok) r2 = {1.f, 0.f};
@@ -629,17 +632,13 @@ __device__ __forceinline__ void pair_t_ds(const float4 &xg, const float4 &Gg, co
     float qe = __fmaf_rn(p, y0, -q);
     qe = __fmaf_rn(pe, y0, qe);                    // r2 y0^2 = q + qe
     const float e = __fsub_rn(__fsub_rn(1.0f, q), qe);
-    dsf y = ds_fast(y0, __fmul_rn(__fmul_rn(0.5f, y0), e));
-    if (!ok) y = {0.f, 0.f};
-    dsf g1 = ds_norm(ds_add_u({Ga.x, Ga.z}, {-Gg.x, -Gg.z}));
-    dsf g2 = ds_norm(ds_add_u({Ga.y, Ga.w}, {-Gg.y, -Gg.w}));
-    dsf dg = ds_add_u(ds_mul_u(d1, g1), ds_mul_u(d2, g2));
-    dsf cc = ds_mul_u(dg, ds_sqr_u(y));
-    dsf m1 = ds_mul_u(d1, cc), m2 = ds_mul_u(d2, cc);
-    t1 = ds_add_u(g1, {-m1.h, -m1.l});
-    t2 = ds_add_u(g2, {-m2.h, -m2.l});
-    wya = ds_mul(wa, y);
-    wyg = ds_mul(wg, y);
+    const dsf y = ds_fast(y0, __fmul_rn(__fmul_rn(0.5f, y0), e));
+    const dsf g1 = ds_norm(ds_add_u({Ga.x, Ga.z}, {-Gg.x, -Gg.z}));
+    const dsf g2 = ds_norm(ds_add_u({Ga.y, Ga.w}, {-Gg.y, -Gg.w}));
+    const dsf m2 = ds_mul_u(g2, d1);
+    const dsf c = ds_norm(ds_add_u(ds_mul_u(g1, d2), {-m2.h, -m2.l}));
+    s = ds_mul_u(c, ds_mul_u(ds_sqr_u(y), y));
+    if (!ok) s = {0.f, 0.f};
 }
 
 __global__ void __launch_bounds__(ST)
@@ -667,10 +666,11 @@ k_pair_ds_sym(const float4 *__restrict__ pfx, const float4 *__restrict__ pfg,
         __syncthreads();
         if (k == 0) {
             for (int a = 0; a < ST; a++) {
-                dsf t1, t2, wya, wyg;
-                pair_t_ds(xg, Gg, sx[a], sg[a], {sw[a].x, sw[a].y}, wg, t1, t2, wya, wyg);
-                ds_acc(ga1, ds_mul_u(wya, t1));
-                ds_acc(ga2, ds_mul_u(wya, t2));
+                dsf d1, d2, sp;
+                pair_s_ds(xg, Gg, sx[a], sg[a], d1, d2, sp);
+                const dsf ws = ds_mul_u({sw[a].x, sw[a].y}, sp);
+                ds_acc(ga1, ds_mul_u(ws, d2));
+                ds_acc(ga2, ds_mul_u(ws, {-d1.h, -d1.l}));
                 if ((a & 31) == 31) {
                     ga1 = ds_norm(ga1);
                     ga2 = ds_norm(ga2);
@@ -684,13 +684,15 @@ k_pair_ds_sym(const float4 *__restrict__ pfx, const float4 *__restrict__ pfg,
 #pragma unroll 2
                 for (int q = 0; q < 32; q++) {
                     const int ai = base + ((lane + q) & 31);
-                    dsf t1, t2, wya, wyg;
-                    pair_t_ds(xg, Gg, sx[ai], sg[ai], {sw[ai].x, sw[ai].y}, wg, t1, t2, wya, wyg);
-                    ds_acc(ga1, ds_mul_u(wya, t1));
-                    ds_acc(ga2, ds_mul_u(wya, t2));
-                    const dsf nw = {-wyg.h, -wyg.l};
-                    ds_acc(a1, ds_mul_u(nw, t1));
-                    ds_acc(a2, ds_mul_u(nw, t2));
+                    dsf d1, d2, sp;
+                    pair_s_ds(xg, Gg, sx[ai], sg[ai], d1, d2, sp);
+                    const dsf ws = ds_mul_u({sw[ai].x, sw[ai].y}, sp);   // w_a s
+                    const dsf wn = ds_mul_u({-wg.h, -wg.l}, sp);         // -w_g s
+                    const dsf nd1 = {-d1.h, -d1.l};
+                    ds_acc(ga1, ds_mul_u(ws, d2));
+                    ds_acc(ga2, ds_mul_u(ws, nd1));
+                    ds_acc(a1, ds_mul_u(wn, d2));
+                    ds_acc(a2, ds_mul_u(wn, nd1));
                     const int src = (lane + 1) & 31;
                     a1.h = __shfl_sync(0xffffffffu, a1.h, src);
                     a1.l = __shfl_sync(0xffffffffu, a1.l, src);

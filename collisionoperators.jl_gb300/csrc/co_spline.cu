@@ -188,41 +188,58 @@ k_perm(const int *__restrict__ cell, int N, const int *__restrict__ hoff,
     }
 }
 
-// Segmented sum per (cell, local basis j1 + 3 j2): one warp per cell, lane l
-// takes the cell's markers l, l + 32, ... in sorted (index) order and the nine
-// lane sums are combined by a fixed shuffle tree. Cells are very uneven (the
-// central cell of a Gaussian holds ~45x the mean), so the warp, not one thread,
-// walks the segment. Deterministic run to run.
+// Segmented sum per (cell, local basis j1 + 3 j2): one block of 4 warps per
+// cell, thread t takes the cell's markers t, t + 128, ... in sorted (index)
+// order; each warp combines its lanes by a fixed shuffle tree and warp 0 adds
+// the four warp sums in warp order. Cells are very uneven (the central cell of
+// a Gaussian holds ~45x the mean), so four warps share the long segments;
+// empty cells leave at once and warps past the segment's end skip the tree.
+// Deterministic run to run.
 __global__ void __launch_bounds__(128)
 k_cellsum(const int *__restrict__ cstart, const double *__restrict__ sw,
           const double *__restrict__ sphi, int n_el, double *__restrict__ bS) {
-    const int c = blockIdx.x * 4 + (threadIdx.x >> 5);
-    const int lane = threadIdx.x & 31;
+    __shared__ double part[4][9];
+    const int c = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (c >= n_el) return;
     const int p0 = cstart[c], p1 = cstart[c + 1];
+    if (p0 == p1) {
+        if (threadIdx.x < 9) bS[(size_t)c * 9 + threadIdx.x] = 0.0;
+        return;
+    }
     double acc[9];
 #pragma unroll
     for (int j = 0; j < 9; j++) acc[j] = 0.0;
-    for (int p = p0 + lane; p < p1; p += 32) {
-        const double *ph = sphi + (size_t)p * 6;
-        const double w = sw[p];
-        const double a0 = ph[0], a1 = ph[1], a2 = ph[2], b0 = ph[3], b1 = ph[4], b2 = ph[5];
-        acc[0] += w * (a0 * b0);
-        acc[1] += w * (a1 * b0);
-        acc[2] += w * (a2 * b0);
-        acc[3] += w * (a0 * b1);
-        acc[4] += w * (a1 * b1);
-        acc[5] += w * (a2 * b1);
-        acc[6] += w * (a0 * b2);
-        acc[7] += w * (a1 * b2);
-        acc[8] += w * (a2 * b2);
+    const bool active = p0 + warp * 32 < p1;
+    if (active) {
+        for (int p = p0 + threadIdx.x; p < p1; p += 128) {
+            const double *ph = sphi + (size_t)p * 6;
+            const double w = sw[p];
+            // w phi1 once, then nine FMAs: GB300 issues FP64 at 1/64 of the
+            // FP32 rate, and the densest cell is the critical path
+            const double a0 = w * ph[0], a1 = w * ph[1], a2 = w * ph[2];
+            const double b0 = ph[3], b1 = ph[4], b2 = ph[5];
+            acc[0] = fma(a0, b0, acc[0]);
+            acc[1] = fma(a1, b0, acc[1]);
+            acc[2] = fma(a2, b0, acc[2]);
+            acc[3] = fma(a0, b1, acc[3]);
+            acc[4] = fma(a1, b1, acc[4]);
+            acc[5] = fma(a2, b1, acc[5]);
+            acc[6] = fma(a0, b2, acc[6]);
+            acc[7] = fma(a1, b2, acc[7]);
+            acc[8] = fma(a2, b2, acc[8]);
+        }
+#pragma unroll
+        for (int j = 0; j < 9; j++)
+            for (int o = 16; o > 0; o >>= 1) acc[j] += __shfl_down_sync(0xffffffffu, acc[j], o);
     }
+    if (lane == 0)
 #pragma unroll
-    for (int j = 0; j < 9; j++)
-        for (int o = 16; o > 0; o >>= 1) acc[j] += __shfl_down_sync(0xffffffffu, acc[j], o);
-    if (lane == 0) {
-#pragma unroll
-        for (int j = 0; j < 9; j++) bS[(size_t)c * 9 + j] = acc[j];
+        for (int j = 0; j < 9; j++) part[warp][j] = acc[j];
+    __syncthreads();
+    if (threadIdx.x < 9) {
+        const int j = threadIdx.x;
+        bS[(size_t)c * 9 + j] = ((part[0][j] + part[1][j]) + part[2][j]) + part[3][j];
     }
 }
 
@@ -245,91 +262,116 @@ __global__ void k_dofgather(const double *__restrict__ src, int n1, int n2, int 
     out[k] = acc;
 }
 
-// y[:, i2] = M1^{-1} b[:, i2]
-__global__ void k_mass1(const double *__restrict__ Minv1, const double *__restrict__ b, int nd1,
-                        int nd2, double *__restrict__ y) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
+// The mass solve f = M1^{-1} B M2^{-1} (M = M2 (x) M1, first index fastest) as
+// two dense products with the 1D inverses. One warp per output: lane l adds the
+// terms k = l, l + 32, ... and a fixed shuffle tree sums the lanes, so the
+// dependent chain is ~nd/32 FMAs long instead of nd, and each warp keeps few
+// loads in flight instead of one thread walking a whole row.
+// y[i1, i2] = sum_k M1^{-1}[i1, k] b[k, i2]
+__global__ void __launch_bounds__(256)
+k_mass1(const double *__restrict__ Minv1, const double *__restrict__ b, int nd1, int nd2,
+        double *__restrict__ y) {
+    const int t = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (t >= nd1 * nd2) return;
-    int i1 = t % nd1, i2 = t / nd1;
-    // Minv1 is exactly symmetric (symmetrised at set-up), so its row i1 is read
-    // as column i1: consecutive threads read consecutive addresses (the same
-    // products in the same order as the row form)
+    const int i1 = t % nd1, i2 = t / nd1;
     const double *col = b + (size_t)i2 * nd1;
     double s = 0.0;
-    for (int k = 0; k < nd1; k++) s = fma(Minv1[(size_t)k * nd1 + i1], col[k], s);
-    y[t] = s;
+    // Minv1 is exactly symmetric (symmetrised at set-up): row i1 read as column i1
+    for (int k = lane; k < nd1; k += 32) s = fma(Minv1[(size_t)k * nd1 + i1], col[k], s);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) y[t] = s;
 }
 
-// out[i1, :] = y[i1, :] M2^{-1}
-__global__ void k_mass2(const double *__restrict__ Minv2, const double *__restrict__ y, int nd1,
-                        int nd2, double *__restrict__ out) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
+// out[i1, i2] = sum_k y[i1, k] M2^{-1}[k, i2]
+__global__ void __launch_bounds__(256)
+k_mass2(const double *__restrict__ Minv2, const double *__restrict__ y, int nd1, int nd2,
+        double *__restrict__ out) {
+    const int t = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (t >= nd1 * nd2) return;
-    int i1 = t % nd1, i2 = t / nd1;
+    const int i1 = t % nd1, i2 = t / nd1;
     double s = 0.0;
-    for (int k = 0; k < nd2; k++) s = fma(y[(size_t)k * nd1 + i1], Minv2[(size_t)k * nd2 + i2], s);
-    out[t] = s;
+    for (int k = lane; k < nd2; k += 32)
+        s = fma(y[(size_t)k * nd1 + i1], Minv2[(size_t)k * nd2 + i2], s);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) out[t] = s;
 }
 
-// One block per element: f at the nq x nq Gauss points, then r-local (mode 0)
-// or the entropy partial (mode 1).
-__global__ void __launch_bounds__(64)
+// One warp per element (four per block): f at the nq x nq Gauss points (lane
+// l takes points l and l + 32), then r-local (mode 0) or the entropy partial
+// (mode 1). The field is evaluated in tensor-product form, f = sum_b p2_b
+// (sum_a c_ab p1_a), and a point's nine contributions are h p1_a p2_b with
+// h = integrand * w_q * |e|; nine threads then add the points in point order
+// (fixed, deterministic).
+#define ELEM_PER_BLOCK 4
+__global__ void __launch_bounds__(32 * ELEM_PER_BLOCK)
 k_elem(const double *__restrict__ fc, int n1, int n2, int nd1, int nq,
        const double *__restrict__ Tq1, const double *__restrict__ Tq2,
        const double *__restrict__ qw, const double *__restrict__ bp1,
        const double *__restrict__ bp2, int logsq, int mode, double *__restrict__ E,
        double *__restrict__ Ep) {
-    __shared__ double contrib[64 * 9];
-    __shared__ double cs[9];
-    int e = blockIdx.x;
-    int i = e % n1, j = e / n1;
-    int t = threadIdx.x;
-    if (t < 9) cs[t] = fc[(i + t % 3) + (j + t / 3) * nd1];
-    __syncthreads();
-    int nqq = nq * nq;
-    double jac = (bp1[i + 1] - bp1[i]) * (bp2[j + 1] - bp2[j]);
-    if (t < nqq) {
-        int q1 = t % nq, q2 = t / nq;
-        double p1[3], p2[3], phi[9];
-        for (int a = 0; a < 3; a++) {
-            p1[a] = Tq1[((size_t)i * 3 + a) * nq + q1];
-            p2[a] = Tq2[((size_t)j * 3 + a) * nq + q2];
-        }
-        double f = 0.0;
-        for (int b = 0; b < 3; b++)
+    __shared__ double contrib[ELEM_PER_BLOCK][64 * 9];
+    __shared__ double cs[ELEM_PER_BLOCK][9];
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    const int e = blockIdx.x * ELEM_PER_BLOCK + wl;
+    const bool live = e < n1 * n2;
+    const int i = live ? e % n1 : 0, j = live ? e / n1 : 0;
+    if (live && lane < 9) cs[wl][lane] = fc[(i + lane % 3) + (j + lane / 3) * nd1];
+    __syncwarp();
+    const int nqq = nq * nq;
+    if (live) {
+        const double jac = (bp1[i + 1] - bp1[i]) * (bp2[j + 1] - bp2[j]);
+        for (int t = lane; t < nqq; t += 32) {
+            const int q1 = t % nq, q2 = t / nq;
+            double p1[3], p2[3];
             for (int a = 0; a < 3; a++) {
-                phi[a + 3 * b] = p1[a] * p2[b];
-                f += cs[a + 3 * b] * phi[a + 3 * b];
+                p1[a] = Tq1[((size_t)i * 3 + a) * nq + q1];
+                p2[a] = Tq2[((size_t)j * 3 + a) * nq + q2];
             }
-        double wq = qw[q1] * qw[q2];
-        if (mode == 0) {
-            double integrand;
-            if (logsq)
-                integrand = f * f > 1e-60 ? (1 + 0.5 * log(f * f)) : 0.0;
-            else
-                integrand = f > 1e-30 ? (1 + log(f)) : 0.0;
-            for (int k = 0; k < 9; k++) contrib[t * 9 + k] = integrand * phi[k] * wq * jac;
-        } else {
-            double s = 0.0;
-            if (logsq) {
-                if (f * f > 1e-60) s = -(f * 0.5 * log(f * f) * wq * jac);
-            } else if (f > 1e-30) {
-                s = -(f * log(f) * wq * jac);
+            double f = 0.0;
+            for (int bb = 0; bb < 3; bb++) {
+                double g = cs[wl][3 * bb] * p1[0];
+                g = fma(cs[wl][3 * bb + 1], p1[1], g);
+                g = fma(cs[wl][3 * bb + 2], p1[2], g);
+                f = fma(g, p2[bb], f);
             }
-            contrib[t] = s;
+            const double wj = qw[q1] * qw[q2] * jac;
+            if (mode == 0) {
+                double integrand;
+                if (logsq)
+                    integrand = f * f > 1e-60 ? (1 + 0.5 * log(f * f)) : 0.0;
+                else
+                    integrand = f > 1e-30 ? (1 + log(f)) : 0.0;
+                const double h = integrand * wj;
+                const double h0 = h * p1[0], h1 = h * p1[1], h2 = h * p1[2];
+                double *o = &contrib[wl][t * 9];
+                for (int bb = 0; bb < 3; bb++) {
+                    o[3 * bb] = h0 * p2[bb];
+                    o[3 * bb + 1] = h1 * p2[bb];
+                    o[3 * bb + 2] = h2 * p2[bb];
+                }
+            } else {
+                double sv = 0.0;
+                if (logsq) {
+                    if (f * f > 1e-60) sv = -(f * 0.5 * log(f * f) * wj);
+                } else if (f > 1e-30) {
+                    sv = -(f * log(f) * wj);
+                }
+                contrib[wl][t] = sv;
+            }
         }
     }
-    __syncthreads();
+    __syncwarp();
+    if (!live) return;
     if (mode == 0) {
-        if (t < 9) {
-            double s = 0.0;
-            for (int q = 0; q < nqq; q++) s += contrib[q * 9 + t];
-            E[(size_t)e * 9 + t] = s;
+        if (lane < 9) {
+            double sum = 0.0;
+            for (int q = 0; q < nqq; q++) sum += contrib[wl][q * 9 + lane];
+            E[(size_t)e * 9 + lane] = sum;
         }
-    } else if (t == 0) {
-        double s = 0.0;
-        for (int q = 0; q < nqq; q++) s += contrib[q];
-        Ep[e] = s;
+    } else if (lane == 0) {
+        double sum = 0.0;
+        for (int q = 0; q < nqq; q++) sum += contrib[wl][q];
+        Ep[e] = sum;
     }
 }
 
@@ -694,9 +736,9 @@ int co_sort_markers(co_ctx *c, const double *x, int N) {
 
 int co_mass_solve_dev(co_ctx *c, const double *rhs, double *out) {
     int n = c->n_dofs;
-    // one warp per block: the FP64 dot products spread over all SMs
-    k_mass1<<<co_cdiv(n, 32), 32, 0, c->stream>>>(c->Minv1, rhs, c->nd1, c->nd2, c->y);
-    k_mass2<<<co_cdiv(n, 32), 32, 0, c->stream>>>(c->Minv2, c->y, c->nd1, c->nd2, out);
+    // one warp per output, eight per block
+    k_mass1<<<co_cdiv(n, 8), 256, 0, c->stream>>>(c->Minv1, rhs, c->nd1, c->nd2, c->y);
+    k_mass2<<<co_cdiv(n, 8), 256, 0, c->stream>>>(c->Minv2, c->y, c->nd1, c->nd2, out);
     c->launches += 2;
     CO_CK(cudaGetLastError());
     return CO_OK;
@@ -704,7 +746,7 @@ int co_mass_solve_dev(co_ctx *c, const double *rhs, double *out) {
 
 // after co_sort_markers: b = scatter, f = M^{-1} b
 int co_project_sorted(co_ctx *c, double *f_out) {
-    k_cellsum<<<co_cdiv(c->n_el, 4), 128, 0, c->stream>>>(c->mb.cstart, c->mb.sw, c->mb.sphi,
+    k_cellsum<<<c->n_el, 128, 0, c->stream>>>(c->mb.cstart, c->mb.sw, c->mb.sphi,
                                                           c->n_el, c->bS);
     k_dofgather<<<co_cdiv(c->n_dofs, 128), 128, 0, c->stream>>>(c->bS, c->n1, c->n2, c->nd1,
                                                                 c->nd2, c->b);
@@ -714,9 +756,9 @@ int co_project_sorted(co_ctx *c, double *f_out) {
 }
 
 int co_compute_r_dev(co_ctx *c, const double *f, double *r) {
-    k_elem<<<c->n_el, 64, 0, c->stream>>>(f, c->n1, c->n2, c->nd1, c->nq, c->Tq1, c->Tq2, c->qw,
-                                          c->bp1, c->bp2, (c->flags & CO_FLAG_LOGSQ) ? 1 : 0, 0,
-                                          c->E, nullptr);
+    k_elem<<<co_cdiv(c->n_el, ELEM_PER_BLOCK), 32 * ELEM_PER_BLOCK, 0, c->stream>>>(
+        f, c->n1, c->n2, c->nd1, c->nq, c->Tq1, c->Tq2, c->qw, c->bp1, c->bp2,
+        (c->flags & CO_FLAG_LOGSQ) ? 1 : 0, 0, c->E, nullptr);
     k_dofgather<<<co_cdiv(c->n_dofs, 128), 128, 0, c->stream>>>(c->E, c->n1, c->n2, c->nd1,
                                                                 c->nd2, r);
     c->launches += 2;
@@ -725,9 +767,9 @@ int co_compute_r_dev(co_ctx *c, const double *f, double *r) {
 }
 
 int co_entropy_parts_dev(co_ctx *c, const double *f) {
-    k_elem<<<c->n_el, 64, 0, c->stream>>>(f, c->n1, c->n2, c->nd1, c->nq, c->Tq1, c->Tq2, c->qw,
-                                          c->bp1, c->bp2, (c->flags & CO_FLAG_LOGSQ) ? 1 : 0, 1,
-                                          nullptr, c->Ep);
+    k_elem<<<co_cdiv(c->n_el, ELEM_PER_BLOCK), 32 * ELEM_PER_BLOCK, 0, c->stream>>>(
+        f, c->n1, c->n2, c->nd1, c->nq, c->Tq1, c->Tq2, c->qw, c->bp1, c->bp2,
+        (c->flags & CO_FLAG_LOGSQ) ? 1 : 0, 1, nullptr, c->Ep);
     c->launches++;
     CO_CK(cudaGetLastError());
     return CO_OK;

@@ -103,13 +103,12 @@ def test_learned_warm_start_small(built_lib, collops_mod, tmp_path):
 
 def test_trained_warm_start_gain(built_lib, collops_mod):
     """The committed network (trained by collops.train_warmstart on >= 1M pairs
-    from the N = 131,072 workload and the batched family) on held-out Landau
-    instances of that family: its proposal's first residual is well below the
-    explicit predictor's. The solve from each start is reported beside it; the
-    first-residual gain is what the network buys (a few outer iterations at most,
-    since each defect-correction outer map cuts the residual ~5x)."""
-    import ctypes as C
-
+    from converged steps of the N = 131,072 workload and the batched family,
+    use_logsq = true) on held-out Landau instances of that family: its proposal's
+    first residual is well below both fallbacks the benchmark spec names -- the
+    explicit predictor and the plain previous-step guess -- and the step from the
+    chosen start converges. The first residuals come from one co_step_learned
+    call (r_start: predictor, learned, previous state)."""
     import torch
     from collops import learned
     path = os.path.join(PKG, "collops", "warmstart_c3.npz")
@@ -119,7 +118,8 @@ def test_trained_warm_start_gain(built_lib, collops_mod):
         bp = uniform_bp(-6.0, 6.0, n)
         v, w = gaussian_markers(N, sx, sy, seed=seed)
         p = collops_mod.SimParameters(bp1=bp, bp2=bp, m_anderson=8, damping=0.7, tol=1e-12,
-                                      abs_floor=0.0, max_iter=400, precision="mixed_ds")
+                                      abs_floor=1e-10, max_iter=400, precision="mixed_ds",
+                                      use_logsq=True)
         ws = collops_mod.build_workspace(p)
         o = p.opts()
         dt = 0.02
@@ -127,24 +127,15 @@ def test_trained_warm_start_gain(built_lib, collops_mod):
         wd = torch.from_numpy(w).cuda()
         S0 = learned.entropy_of(ws, x, wd)
         v1 = torch.empty_like(x)
-        used, rl, rp = warm.propose(ws, o, x, wd, S0, dt, v1)
-        _X, vp, _rp = learned.features(ws, o, x, wd, S0, dt)
-        its = []
-        for start in (v1.clone(), vp.clone()):
-            it, inner = C.c_int(), C.c_int()
-            res, r0 = C.c_double(), C.c_double()
-            d = collops_mod.CoDefectOpts(0.05, 60, 5, 0.5, 0, 0, 0, 1e-2)
-            oo = p.opts()
-            oo.stag_rel_tol = 0.1
-            collops_mod._check(ws.lib.co_step_defect_dev(
-                ws.h, C.byref(oo), C.byref(d), start.data_ptr(), x.data_ptr(), wd.data_ptr(), N,
-                S0, dt, C.byref(it), C.byref(res), C.byref(inner), C.byref(r0)), "defect")
-            its.append((it.value, inner.value, res.value))
+        d = collops_mod.CoDefectOpts(0.02, 100, 5, 0.9, 0, 5, 0, 1e-3, 0)
+        rec = warm.step(ws, o, d, x, wd, S0, dt, v1)
         ws.close()
-        print(f"N={N}: first residual learned {rl:.3e} predictor {rp:.3e} (x{rp / rl:.2f}); "
-              f"outer/inner learned {its[0][:2]} predictor {its[1][:2]}")
-        assert used and rl < 0.8 * rp
-        gains.append(rp / rl)
+        r_pred, r_learn, r_prev = rec["r_start"]
+        print(f"N={N}: first residual learned {r_learn:.3e} predictor {r_pred:.3e} "
+              f"previous {r_prev:.3e}; start {rec['start']}, outer {rec['outer']}, "
+              f"inner {rec['inner']}, converged {rec['converged']}")
+        assert rec["start"] == "learned" and rec["converged"]
+        gains.append(min(r_pred, r_prev) / r_learn)
     warm.mlp.close()
     assert min(gains) > 1.25
 
