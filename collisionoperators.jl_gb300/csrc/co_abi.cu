@@ -171,7 +171,8 @@ extern "C" const char *co_strerror(int s) {
 
 static void free_ctx(co_ctx *c) {
     if (!c) return;
-    void *ptrs[] = {c->bp1, c->bp2, c->C1, c->C2, c->Tq1, c->Tq2, c->qw, c->Minv1, c->Minv2,
+    void *ptrs[] = {c->bp1, c->bp2, c->C1, c->C2, c->Tq1, c->Tq2, c->ih1, c->ih2, c->P1, c->P2,
+                    c->qw, c->Minv1, c->Minv2,
                     c->bS, c->b, c->y, c->f, c->fin, c->rr, c->L, c->E, c->Ep, c->st,
                     c->mb.vmid, c->mb.dv, c->mb.G, c->mb.dS, c->mb.Gv, c->mb.r, c->mb.rp,
                     c->mb.Gp, c->mb.vbest, c->mb.v1, c->mb.v0, c->mb.w, c->mb.vin, c->mb.dotv,
@@ -184,6 +185,7 @@ static void free_ctx(co_ctx *c) {
         if (p) cudaFree(p);
     co_step_free(c);
     co_newton_free(c);
+    co_sortset_free(c);
     co_prof_free(c);
     if (c->st_host) cudaFreeHost(c->st_host);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -253,6 +255,35 @@ extern "C" int co_ctx_create(const double *bp1, int nb1, const double *bp2, int 
             phi_at(&C2[9 * (size_t)e], qx[q], phi);
             for (int a = 0; a < 3; a++) T2[((size_t)e * 3 + a) * n_quad + q] = phi[a];
         }
+    // per-cell tables of the marker kernels (locate, sort, grad L): the
+    // reciprocal widths, and each cell-local basis function
+    // p_j(x) = sum_k C[k][j] B_k(x) with B = ((1-x)^2, 2x(1-x), x^2) rewritten
+    // as alpha + beta x + gamma x^2, so that p and dp/dx cost 3 FMAs on the
+    // device instead of the Bernstein values plus the 3x3 extraction product
+    auto cell_tables = [](const std::vector<double> &B, const std::vector<double> &C, int n,
+                          std::vector<double> &ih, std::vector<double> &P) {
+        ih.resize(n);
+        P.resize((size_t)n * 12);
+        for (int e = 0; e < n; e++) {
+            ih[e] = 1.0 / (B[e + 1] - B[e]);
+            for (int j = 0; j < 3; j++) {
+                const double c0 = C[9 * (size_t)e + j], c1 = C[9 * (size_t)e + 3 + j],
+                             c2 = C[9 * (size_t)e + 6 + j];
+                const double gam = (c0 - 2.0 * c1) + c2;
+                P[12 * (size_t)e + 4 * j + 0] = c0;
+                P[12 * (size_t)e + 4 * j + 1] = 2.0 * (c1 - c0);
+                P[12 * (size_t)e + 4 * j + 2] = gam;
+                P[12 * (size_t)e + 4 * j + 3] = 2.0 * gam;
+            }
+        }
+    };
+    std::vector<double> IH1, IH2, P1, P2;
+    cell_tables(B1, C1, c->n1, IH1, P1);
+    cell_tables(B2, C2, c->n2, IH2, P2);
+    TRY(upload(&c->ih1, IH1));
+    TRY(upload(&c->ih2, IH2));
+    TRY(upload(&c->P1, P1));
+    TRY(upload(&c->P2, P2));
     mass1d(B1, C1, M1);
     mass1d(B2, C2, M2);
     TRY(spd_inverse(M1, c->nd1, I1));

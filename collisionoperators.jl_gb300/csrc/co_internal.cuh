@@ -85,6 +85,16 @@ struct co_bufs {
     double *pc;
 };
 
+// Buffers of one counting sort + projection (co_spline.cu). Set 0 is the
+// context's primary set (mb.cell ... mb.sphi, bS, b, y); set 1 (ctx.gs) holds
+// the second marker set of the Gonzalez chain -- v_in, whose entropy S(v_in)
+// is needed beside the v_mid projection -- sorted and projected in the same
+// launches as set 0 (blockIdx.y selects the set).
+struct co_sortset {
+    int *cell, *inv, *perm, *scell, *hist, *hoff, *count, *cstart;
+    double *xi, *sw, *sphi, *bS, *b, *y;
+};
+
 struct co_ctx {
     int device;
     cudaStream_t stream;
@@ -95,6 +105,9 @@ struct co_ctx {
     double *bp1, *bp2;       // breakpoints
     double *C1, *C2;         // extraction [n][9]
     double *Tq1, *Tq2;       // basis at quad nodes: [n][3][nq]
+    double *ih1, *ih2;       // reciprocal cell widths 1 / (bp[i+1] - bp[i])
+    double *P1, *P2;         // cell-local basis C^T B in monomial form: [n][3][4] =
+                             // (alpha, beta, gamma, 2 gamma), p = alpha + beta x + gamma x^2
     double *qw;              // quad weights [nq]
     double *Minv1, *Minv2;   // inverse 1D mass matrices (nd x nd, symmetric)
     // coefficient-sized buffers
@@ -102,6 +115,8 @@ struct co_ctx {
     double *b, *y, *f, *fin, *rr, *L;  // n_dofs each
     double *E;               // element-local r contributions [n_el][9]
     double *Ep;              // element entropy partials [n_el]
+    co_sortset gs;           // sort/projection set 1 (Gonzalez v_in), allocated on use
+    int gs_cap;              // marker capacity of gs (0: not allocated)
     co_bufs mb;
     co_solver_state *st;     // device state
     co_solver_state *st2;    // inner-solve state of the defect correction
@@ -141,6 +156,15 @@ static inline int co_cdiv(long long a, long long b) { return (int)((a + b - 1) /
 // (co_spline.cu)
 int co_ensure_capacity(co_ctx *c, int N, int m);
 int co_sort_markers(co_ctx *c, const double *x, int N);       // locate + stable cell sort
+// v_mid = (v0 + v_in)/2 and dv = v_in - v0 into mb.vmid/mb.dv, v_mid sorted into
+// set 0 and, with two != 0, v_in sorted into set 1, in the same launches
+int co_sort_mid(co_ctx *c, const double *vin, const double *v0, int N, int two);
+// co_project_sorted for set 0 -> f0 and (two != 0) set 1 -> f1
+int co_project_two(co_ctx *c, double *f0, double *f1, int two);
+// r-local of f (-> dof vector r) and, with fS != nullptr, the entropy partials of
+// fS (-> Ep), in one quadrature launch
+int co_r_and_entropy_dev(co_ctx *c, const double *f, double *r, const double *fS);
+void co_sortset_free(co_ctx *c);
 int co_project_sorted(co_ctx *c, double *f_out);               // scatter + dof gather + mass solve
 int co_mass_solve_dev(co_ctx *c, const double *rhs, double *out);
 int co_compute_r_dev(co_ctx *c, const double *f, double *r);
@@ -150,7 +174,6 @@ int co_grad_L_dev(co_ctx *c, const double *x, int N, const double *L, double *G,
                   const double *w, double *dS, const double *dv, double *red);
 int co_loggrad_dev(co_ctx *c, const double *x, int N, const double *f, double *g,
                    const double *w, const double *dv, double *red);
-int co_mid_dv(co_ctx *c, const double *vin, const double *v0, int N);
 int co_hess_L_dev(co_ctx *c, int N, double *H);
 int co_diagnostics_impl(co_ctx *c, const double *x, int N, double *out6);
 #define CO_WS_NFEAT 15   // warm-start features per marker

@@ -455,8 +455,7 @@ k_anderson_solve(const double *__restrict__ red, int nred, co_solver_state *st, 
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
         for (int c = warp; c < 2 * h; c += nw) {
             const int col = c < h ? c : CO_MAX_M + (c - h);
-            double s = 0.0;
-            for (int i = lane; i < nred; i += 32) s += red[(size_t)i * 2 * CO_MAX_M + col];
+            double s = co_strided_sum(red, lane, nred, 32, 2 * CO_MAX_M, col, 0.0);
             for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
             if (lane == 0) dots[col] = s;
         }
@@ -549,15 +548,6 @@ static int red_blocks(co_ctx *c, int N) {
     return g < 1 ? 1 : g;
 }
 
-// Gonzalez entropy S1 of v_in's projection into st->S1
-static int entropy_into_state(co_ctx *c, const double *x, int N) {
-    int rc;
-    if ((rc = co_sort_markers(c, x, N))) return rc;
-    if ((rc = co_project_sorted(c, c->fin))) return rc;
-    if ((rc = co_entropy_parts_dev(c, c->fin))) return rc;
-    return co_entropy_finalize_dev(c, &c->st->S1);
-}
-
 int co_lb_fused(co_ctx *c, int N, double nu, double dt, double *Gv, const double *v0,
                 const double *vmid, const double *w, double *g, const double *dv,
                 int gonzalez, const double *v1, double *r) {
@@ -590,10 +580,13 @@ int co_lb_fused(co_ctx *c, int N, double nu, double dt, double *Gv, const double
 
 // landau_geff! (solver.jl:86-113) after the v_mid projection: r, L = M^{-1} r,
 // grad L at v_mid with dS = -w G and the Gonzalez partials, then lambda.
+// With gonzalez, the quadrature launch also takes the entropy partials of
+// v_in's projection (c->fin), summed into st->S1 before lambda needs it.
 static int landau_tail(co_ctx *c, int gonzalez, int N, double S0, int nred) {
     int rc;
     co_bufs &b = c->mb;
-    if ((rc = co_compute_r_dev(c, c->f, c->rr))) return rc;
+    if ((rc = co_r_and_entropy_dev(c, c->f, c->rr, gonzalez ? c->fin : nullptr))) return rc;
+    if (gonzalez && (rc = co_entropy_finalize_dev(c, &c->st->S1))) return rc;
     if ((rc = co_mass_solve_dev(c, c->rr, c->L))) return rc;
     if ((rc = co_grad_L_dev(c, b.vmid, N, c->L, b.G, b.w, b.dS, b.dv, b.red))) return rc;
     k_lambda<<<1, 256, 0, c->stream>>>(b.red, nred, c->st, S0, gonzalez);
@@ -602,16 +595,19 @@ static int landau_tail(co_ctx *c, int gonzalez, int N, double S0, int nred) {
     return CO_OK;
 }
 
+// v_mid, dv and the projection of v_mid (set 0 -> c->f) and, with gonzalez, of
+// v_in (set 1 -> c->fin, for S(v_in)), in shared launches
+static int project_mid(co_ctx *c, int gonzalez, const double *vin, const double *v0, int N) {
+    int rc;
+    if ((rc = co_sort_mid(c, vin, v0, N, gonzalez))) return rc;
+    return co_project_two(c, c->f, c->fin, gonzalez);
+}
+
 // full landau_geff! at v_in: leaves dS, dv, lambda (st) and the sorted v_mid
 static int landau_geff_dev(co_ctx *c, int gonzalez, const double *vin, const double *v0, int N,
                            double S0) {
     int rc;
-    co_bufs &b = c->mb;
-    if (gonzalez)
-        if ((rc = entropy_into_state(c, vin, N))) return rc;
-    if ((rc = co_mid_dv(c, vin, v0, N))) return rc;
-    if ((rc = co_sort_markers(c, b.vmid, N))) return rc;
-    if ((rc = co_project_sorted(c, c->f))) return rc;
+    if ((rc = project_mid(c, gonzalez, vin, v0, N))) return rc;
     return landau_tail(c, gonzalez, N, S0, red_blocks(c, N));
 }
 
@@ -623,12 +619,12 @@ static int picard_map_impl(co_ctx *c, int model, int gonzalez, double nu, int pr
     int rc;
     co_bufs &b = c->mb;
     int nred = red_blocks(c, N);
-    if (gonzalez)
-        if ((rc = entropy_into_state(c, vin, N))) return rc;
-    if ((rc = co_mid_dv(c, vin, v0, N))) return rc;
-    if ((rc = co_sort_markers(c, b.vmid, N))) return rc;
-    if ((rc = co_project_sorted(c, c->f))) return rc;
+    if ((rc = project_mid(c, gonzalez, vin, v0, N))) return rc;
     if (model == CO_MODEL_LB) {
+        if (gonzalez) {
+            if ((rc = co_entropy_parts_dev(c, c->fin))) return rc;
+            if ((rc = co_entropy_finalize_dev(c, &c->st->S1))) return rc;
+        }
         if ((rc = co_loggrad_dev(c, b.vmid, N, c->f, b.G, b.w, b.dv, b.red))) return rc;
         k_lambda<<<1, 256, 0, c->stream>>>(b.red, nred, c->st, S0, gonzalez);
         c->launches++;
@@ -1090,6 +1086,19 @@ __global__ void k_copy_if_done(int n2, const co_solver_state *st, int want, doub
         dst[i] = src[i];
 }
 
+// Condition of the device-side inner loop: repeat while the inner solve has not
+// exited (converged, error) and fewer than cap iterations ran.
+__global__ void k_inner_continue(cudaGraphConditionalHandle h, const co_solver_state *si,
+                                 int cap) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    cudaGraphSetConditional(h, (!si->done && !si->error && si->k < cap) ? 1u : 0u);
+}
+
+static bool co_inner_host_loop() {
+    const char *e = getenv("COLLOPS_INNER_LOOP");
+    return e && strcmp(e, "host") == 0;
+}
+
 int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *dopt, int N,
                            double S0, double dt, int *outer, double *res, int *inner,
                            double *r0) {
@@ -1158,6 +1167,82 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
         k_state_reset<<<1, 32, 0, c->stream>>>(c->st3);
         c->launches++;
     }
+    // one inner iteration: G_eff at u, the frozen-metric map Phi(u) and its
+    // residual, the Anderson control and update of u (= v1, in place)
+    auto inner_iteration = [&]() -> int {
+        int rc;
+        if ((rc = landau_geff_dev(c, gz, b.v1, b.v0, N, S0))) return rc;
+        k_frozen_map<<<nred, CO_RED_THREADS, 0, c->stream>>>(N, b.Gv, b.Adef, b.Gk, b.dS, b.dv,
+                                                           b.w, c->st, gz, dt, b.v1, b.Phi, b.r,
+                                                           b.red);
+        // the map Anderson iterates and its residual: Phi, r -- or, with the
+        // preconditioner, Psi = u + P^{-1} r and P^{-1} r
+        double *mapv = b.Phi, *res = b.r;
+        if (pcon) {
+            if ((rc = co_hess_L_dev(c, N, pc_H))) return rc;
+            k_precond<<<co_cdiv(N, 256), 256, 0, c->stream>>>(N, b.Adef, pc_H, b.w, c->st,
+                                                              gz && pcon == 1, dt, b.v1, b.r,
+                                                              pc_z, pc_Psi);
+            c->launches++;
+            mapv = pc_Psi;
+            res = pc_z;
+        }
+        k_ctrl_inner<<<1, 256, 0, c->stream>>>(b.red, nred, c->st2, c->st, o->m, o->damping);
+        k_plain_update<<<eg, 256, 0, c->stream>>>(n2, c->st2, 0, b.v1, mapv, res, b.rp, b.Gp,
+                                                  b.vbest);
+        int ng = red_blocks(c, n2);
+        k_anderson_cols<<<ng, CO_RED_THREADS, 0, c->stream>>>(n2, c->st2, res, b.rp, mapv,
+                                                              b.Gp, b.dF, b.dG, ldF, b.red);
+        k_anderson_solve<<<1, 256, 0, c->stream>>>(b.red, ng, c->st2, di);
+        k_anderson_update<<<eg, 256, 0, c->stream>>>(n2, c->st2, b.v1, mapv, b.dG, ldF);
+        c->launches += 6;
+        CO_CK(cudaGetLastError());
+        return CO_OK;
+    };
+    // The inner loop runs on the device: inner_iteration is captured once per
+    // call as the body of a conditional WHILE node, and k_inner_continue ends it
+    // when the inner solve exits or max_inner iterations ran. The host launches
+    // one graph and waits once per outer iteration instead of once per inner
+    // iteration (COLLOPS_INNER_LOOP=host restores the host-driven loop; both
+    // run the same kernels on the same data and give identical results).
+    const bool host_loop = co_inner_host_loop();
+    struct inner_graph {
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t e = nullptr;
+        unsigned long long body_launches = 0;
+        ~inner_graph() {
+            if (e) cudaGraphExecDestroy(e);
+            if (g) cudaGraphDestroy(g);
+        }
+    } ig;
+    auto capture_inner = [&]() -> int {
+        CO_CK(cudaGraphCreate(&ig.g, 0));
+        cudaGraphConditionalHandle hnd;
+        CO_CK(cudaGraphConditionalHandleCreate(&hnd, ig.g, 1, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams np = {};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = hnd;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t node;
+        CO_CK(cudaGraphAddNode(&node, ig.g, nullptr, nullptr, 0, &np));
+        cudaGraph_t body = np.conditional.phGraph_out[0];
+        CO_CK(cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0,
+                                            cudaStreamCaptureModeThreadLocal));
+        const unsigned long long l0 = c->launches;
+        int r = inner_iteration();
+        if (!r) {
+            k_inner_continue<<<1, 32, 0, c->stream>>>(hnd, c->st2, dopt->max_inner);
+            c->launches++;
+            if (cudaGetLastError() != cudaSuccess) r = CO_ERR_CUDA;
+        }
+        ig.body_launches = c->launches - l0;
+        cudaError_t ce = cudaStreamEndCapture(c->stream, &body);
+        if (r) return r;
+        if (ce != cudaSuccess) return CO_ERR_CUDA;
+        if (cudaGraphInstantiate(&ig.e, ig.g, 0) != cudaSuccess) return CO_ERR_CUDA;
+        return CO_OK;
+    };
     int aa_stage = -1;   // pair precision of the outer map the window was built on
     double first_outer = 0.0, prev_outer = 0.0;   // outer residuals (metric_freeze)
     int k;
@@ -1208,39 +1293,28 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
         // ---- inner: Anderson on the frozen-metric map (u = v1 in place)
         k_state_reset<<<1, 32, 0, c->stream>>>(c->st2);
         c->launches++;
-        int j;
-        for (j = 1; j <= dopt->max_inner; j++) {
-            if ((rc = landau_geff_dev(c, gz, b.v1, b.v0, N, S0))) return rc;
-            k_frozen_map<<<nred, CO_RED_THREADS, 0, c->stream>>>(N, b.Gv, b.Adef, b.Gk, b.dS, b.dv,
-                                                               b.w, c->st, gz, dt, b.v1, b.Phi, b.r,
-                                                               b.red);
-            // the map Anderson iterates and its residual: Phi, r -- or, with the
-            // preconditioner, Psi = u + P^{-1} r and P^{-1} r
-            double *mapv = b.Phi, *res = b.r;
-            if (pcon) {
-                if ((rc = co_hess_L_dev(c, N, pc_H))) return rc;
-                k_precond<<<co_cdiv(N, 256), 256, 0, c->stream>>>(N, b.Adef, pc_H, b.w, c->st,
-                                                                  gz && pcon == 1, dt, b.v1, b.r,
-                                                                  pc_z, pc_Psi);
-                c->launches++;
-                mapv = pc_Psi;
-                res = pc_z;
+        int j;   // inner iterations run (max_inner + 1: the cap was reached)
+        if (host_loop) {
+            for (j = 1; j <= dopt->max_inner; j++) {
+                if ((rc = inner_iteration())) return rc;
+                CO_CK(cudaMemcpyAsync(c->st_host, c->st2, sizeof(co_solver_state),
+                                      cudaMemcpyDeviceToHost, c->stream));
+                CO_CK(cudaStreamSynchronize(c->stream));
+                if (c->st_host->error) return c->st_host->error;
+                if (c->st_host->done) break;
             }
-            k_ctrl_inner<<<1, 256, 0, c->stream>>>(b.red, nred, c->st2, c->st, o->m, o->damping);
-            k_plain_update<<<eg, 256, 0, c->stream>>>(n2, c->st2, 0, b.v1, mapv, res, b.rp, b.Gp,
-                                                      b.vbest);
-            int ng = red_blocks(c, n2);
-            k_anderson_cols<<<ng, CO_RED_THREADS, 0, c->stream>>>(n2, c->st2, res, b.rp, mapv,
-                                                                  b.Gp, b.dF, b.dG, ldF, b.red);
-            k_anderson_solve<<<1, 256, 0, c->stream>>>(b.red, ng, c->st2, di);
-            k_anderson_update<<<eg, 256, 0, c->stream>>>(n2, c->st2, b.v1, mapv, b.dG, ldF);
-            c->launches += 6;
-            CO_CK(cudaGetLastError());
+        } else if (dopt->max_inner < 1) {
+            j = 1;
+        } else {
+            if (!ig.e && (rc = capture_inner())) return rc;
+            CO_CK(cudaGraphLaunch(ig.e, c->stream));
             CO_CK(cudaMemcpyAsync(c->st_host, c->st2, sizeof(co_solver_state),
                                   cudaMemcpyDeviceToHost, c->stream));
             CO_CK(cudaStreamSynchronize(c->stream));
             if (c->st_host->error) return c->st_host->error;
-            if (c->st_host->done) break;
+            const int ran = c->st_host->k;   // k_ctrl_inner counts every iteration
+            c->launches += (unsigned long long)(ran > 1 ? ran - 1 : 0) * ig.body_launches;
+            j = c->st_host->done ? ran : dopt->max_inner + 1;
         }
         total_inner += j > dopt->max_inner ? dopt->max_inner : j;
         if (co_verbose())

@@ -52,68 +52,112 @@ __device__ __forceinline__ int cell_search(const double *__restrict__ bp, int n,
     return lo;
 }
 
-// ---------------------------------------------------------------- kernels
-
-// v_mid = 0.5 (v0 + v_in), dv = v_in - v0  (solver.jl:181-182)
-__global__ void k_mid_dv(const double *__restrict__ vin, const double *__restrict__ v0,
-                         double *__restrict__ vmid, double *__restrict__ dv, int n2) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n2) {
-        double a = vin[i], b = v0[i];
-        vmid[i] = 0.5 * (b + a);
-        dv[i] = a - b;
+// p_j(x) (and dp_j/dx) of the three cell-local basis functions from the cell's
+// monomial table P[j] = (alpha, beta, gamma, 2 gamma): the extraction product
+// C^T B(x) of extract3/bern2 in 2-3 FMAs per function (equal to it within a few
+// ulps; FP64 issue is the bound of the marker kernels on this GPU)
+__device__ __forceinline__ void basis_mono(const double *__restrict__ P, double x, double *p,
+                                           double *dp) {
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        const double *q = P + 4 * j;
+        p[j] = fma(fma(q[2], x, q[1]), x, q[0]);
+        if (dp) dp[j] = fma(q[3], x, q[1]);
     }
 }
 
-// locate_particle (MantisWrappers.jl:168-179) + per-chunk cell histogram.
+// ---------------------------------------------------------------- kernels
+
+// One marker set of a locate launch. With v0 set, x is v_in and the located
+// points are v_mid = 0.5 (v0 + v_in), written to vmid beside dv = v_in - v0
+// (solver.jl:181-182); otherwise x itself is located.
+struct co_locate_job {
+    const double *x, *v0;
+    double *vmid, *dv;
+    int *cell;
+    double *xi;
+    int *hist;
+};
+
+// locate_particle (MantisWrappers.jl:168-179) + per-chunk cell histogram, for
+// one or two marker sets (blockIdx.y). The reference coordinate is (v - bp[i])
+// times the cell's reciprocal width (within one ulp of the quotient; an FP64
+// division costs ~10 FP64 issue slots on this GPU).
 __global__ void __launch_bounds__(CO_CHUNK)
-k_locate_hist(const double *__restrict__ x, int N, const double *__restrict__ bp1, int n1,
-              const double *__restrict__ bp2, int n2, int *__restrict__ cell,
-              double *__restrict__ xi, int *__restrict__ hist, int n_el) {
+k_locate_hist(co_locate_job j0, co_locate_job j1, int N, const double *__restrict__ bp1,
+              int n1, const double *__restrict__ bp2, int n2, const double *__restrict__ ih1,
+              const double *__restrict__ ih2, int n_el) {
     extern __shared__ int hs[];
+    const co_locate_job J = blockIdx.y ? j1 : j0;
     for (int i = threadIdx.x; i < n_el; i += blockDim.x) hs[i] = 0;
     __syncthreads();
     int a = blockIdx.x * CO_CHUNK + threadIdx.x;
     if (a < N) {
-        double v1 = x[a], v2 = x[N + a];
+        double v1 = J.x[a], v2 = J.x[N + a];
+        if (J.v0) {
+            const double b1 = J.v0[a], b2 = J.v0[N + a];
+            const double m1 = 0.5 * (b1 + v1), m2 = 0.5 * (b2 + v2);
+            J.vmid[a] = m1;
+            J.vmid[N + a] = m2;
+            J.dv[a] = v1 - b1;
+            J.dv[N + a] = v2 - b2;
+            v1 = m1;
+            v2 = m2;
+        }
         int c = -1;
         double x1 = 0.0, x2 = 0.0;
         if (!(v1 <= bp1[0] || v1 >= bp1[n1] || v2 <= bp2[0] || v2 >= bp2[n2])) {
             int i = cell_search(bp1, n1, v1);
             int j = cell_search(bp2, n2, v2);
-            x1 = (v1 - bp1[i]) / (bp1[i + 1] - bp1[i]);
-            x2 = (v2 - bp2[j]) / (bp2[j + 1] - bp2[j]);
+            x1 = (v1 - bp1[i]) * ih1[i];
+            x2 = (v2 - bp2[j]) * ih2[j];
             c = i + j * n1;
             atomicAdd(&hs[c], 1);
         }
-        cell[a] = c;
-        xi[a] = x1;
-        xi[N + a] = x2;
+        J.cell[a] = c;
+        J.xi[a] = x1;
+        J.xi[N + a] = x2;
     }
     __syncthreads();
-    if (hist)
-        for (int i = threadIdx.x; i < n_el; i += blockDim.x)
-            hist[(size_t)blockIdx.x * n_el + i] = hs[i];
+    for (int i = threadIdx.x; i < n_el; i += blockDim.x)
+        J.hist[(size_t)blockIdx.x * n_el + i] = hs[i];
 }
 
 // per cell: exclusive offsets of each chunk within the cell, and the count
-__global__ void k_cellcount(const int *__restrict__ hist, int nchunk, int n_el,
-                            int *__restrict__ hoff, int *__restrict__ count) {
+__global__ void k_cellcount(co_sortset s0, co_sortset s1, int nchunk, int n_el) {
+    const co_sortset S = blockIdx.y ? s1 : s0;
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n_el) return;
-    int run = 0;
-    for (int k = 0; k < nchunk; k++) {
+    const int *__restrict__ hist = S.hist;
+    int *__restrict__ hoff = S.hoff;
+    int run = 0, k = 0;
+    // eight chunk counts loaded ahead of the running sum: one L2 round trip
+    // per eight chunks instead of per chunk
+    for (; k + 8 <= nchunk; k += 8) {
+        int h[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) h[u] = hist[(size_t)(k + u) * n_el + c];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            hoff[(size_t)(k + u) * n_el + c] = run;
+            run += h[u];
+        }
+    }
+    for (; k < nchunk; k++) {
         int h = hist[(size_t)k * n_el + c];
         hoff[(size_t)k * n_el + c] = run;
         run += h;
     }
-    count[c] = run;
+    S.count[c] = run;
 }
 
-// exclusive scan of count[0..n) -> cstart[0..n]; one block of 1024 threads
+// exclusive scan of count[0..n) -> cstart[0..n]; one block of 1024 threads per set
 __global__ void __launch_bounds__(1024)
-k_cellscan(const int *__restrict__ count, int n, int *__restrict__ cstart) {
+k_cellscan(co_sortset s0, co_sortset s1, int n) {
     __shared__ int sh[1024];
+    const co_sortset S = blockIdx.y ? s1 : s0;
+    const int *__restrict__ count = S.count;
+    int *__restrict__ cstart = S.cstart;
     int per = (n + 1023) / 1024;
     int t = threadIdx.x;
     int b0 = t * per, b1 = min(n, b0 + per);
@@ -137,18 +181,18 @@ k_cellscan(const int *__restrict__ count, int n, int *__restrict__ cstart) {
 }
 
 // Stable placement: rank of each marker among the markers of its cell that
-// precede it in its chunk, warps taking turns in index order.
+// precede it in its chunk, warps taking turns in index order. The sorted
+// weights and the six cell-local basis values per marker are written for the
+// scatter.
 __global__ void __launch_bounds__(CO_CHUNK)
-k_perm(const int *__restrict__ cell, int N, const int *__restrict__ hoff,
-       const int *__restrict__ cstart, int n_el, int n1, const double *__restrict__ w,
-       const double *__restrict__ xi, const double *__restrict__ C1,
-       const double *__restrict__ C2, int *__restrict__ perm, int *__restrict__ inv,
-       int *__restrict__ scell, double *__restrict__ sw, double *__restrict__ sphi) {
+k_perm(co_sortset s0, co_sortset s1, int N, int n_el, int n1, const double *__restrict__ w,
+       const double *__restrict__ P1, const double *__restrict__ P2) {
     extern __shared__ int run[];
+    const co_sortset S = blockIdx.y ? s1 : s0;
     for (int i = threadIdx.x; i < n_el; i += blockDim.x) run[i] = 0;
     __syncthreads();
     int a = blockIdx.x * CO_CHUNK + threadIdx.x;
-    int c = a < N ? cell[a] : -2;
+    int c = a < N ? S.cell[a] : -2;
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned peers = __match_any_sync(0xffffffffu, c);
     int rank = __popc(peers & ((1u << lane) - 1u));
@@ -167,25 +211,18 @@ k_perm(const int *__restrict__ cell, int N, const int *__restrict__ hoff,
     }
     if (a >= N) return;
     if (c < 0) {
-        inv[a] = -1;
+        S.inv[a] = -1;
         return;
     }
-    int pos = cstart[c] + hoff[(size_t)blockIdx.x * n_el + c] + base + rank;
-    perm[pos] = a;
-    inv[a] = pos;
-    scell[pos] = c;
-    sw[pos] = w[a];
-    if (sphi) {
-        int i = c % n1, j = c / n1;
-        double B[3], p[3];
-        bern2(xi[a], B, nullptr);
-        extract3(C1 + 9 * i, B, p);
-        double *o = sphi + (size_t)pos * 6;
-        o[0] = p[0]; o[1] = p[1]; o[2] = p[2];
-        bern2(xi[N + a], B, nullptr);
-        extract3(C2 + 9 * j, B, p);
-        o[3] = p[0]; o[4] = p[1]; o[5] = p[2];
-    }
+    int pos = S.cstart[c] + S.hoff[(size_t)blockIdx.x * n_el + c] + base + rank;
+    S.perm[pos] = a;
+    S.inv[a] = pos;
+    S.scell[pos] = c;
+    S.sw[pos] = w[a];
+    int i = c % n1, j = c / n1;
+    double *o = S.sphi + (size_t)pos * 6;
+    basis_mono(P1 + 12 * i, S.xi[a], o, nullptr);
+    basis_mono(P2 + 12 * j, S.xi[N + a], o + 3, nullptr);
 }
 
 // Segmented sum per (cell, local basis j1 + 3 j2): one block of 4 warps per
@@ -196,13 +233,16 @@ k_perm(const int *__restrict__ cell, int N, const int *__restrict__ hoff,
 // empty cells leave at once and warps past the segment's end skip the tree.
 // Deterministic run to run.
 __global__ void __launch_bounds__(128)
-k_cellsum(const int *__restrict__ cstart, const double *__restrict__ sw,
-          const double *__restrict__ sphi, int n_el, double *__restrict__ bS) {
+k_cellsum(co_sortset s0, co_sortset s1, int n_el) {
     __shared__ double part[4][9];
+    const co_sortset S = blockIdx.y ? s1 : s0;
     const int c = blockIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (c >= n_el) return;
-    const int p0 = cstart[c], p1 = cstart[c + 1];
+    const double *__restrict__ sw = S.sw;
+    const double *__restrict__ sphi = S.sphi;
+    double *__restrict__ bS = S.bS;
+    const int p0 = S.cstart[c], p1 = S.cstart[c + 1];
     if (p0 == p1) {
         if (threadIdx.x < 9) bS[(size_t)c * 9 + threadIdx.x] = 0.0;
         return;
@@ -243,9 +283,13 @@ k_cellsum(const int *__restrict__ cstart, const double *__restrict__ sw,
     }
 }
 
-// dof k = (k1, k2) gathers the <= 9 cell-local entries that touch it
-__global__ void k_dofgather(const double *__restrict__ src, int n1, int n2, int nd1, int nd2,
-                            double *__restrict__ out) {
+// dof k = (k1, k2) gathers the <= 9 cell-local entries that touch it; one or
+// two (src, out) pairs (blockIdx.y)
+__global__ void k_dofgather(const double *__restrict__ src0, double *__restrict__ out0,
+                            const double *__restrict__ src1, double *__restrict__ out1, int n1,
+                            int n2, int nd1, int nd2) {
+    const double *__restrict__ src = blockIdx.y ? src1 : src0;
+    double *__restrict__ out = blockIdx.y ? out1 : out0;
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nd1 * nd2) return;
     int k1 = k % nd1, k2 = k / nd1;
@@ -266,11 +310,15 @@ __global__ void k_dofgather(const double *__restrict__ src, int n1, int n2, int 
 // two dense products with the 1D inverses. One warp per output: lane l adds the
 // terms k = l, l + 32, ... and a fixed shuffle tree sums the lanes, so the
 // dependent chain is ~nd/32 FMAs long instead of nd, and each warp keeps few
-// loads in flight instead of one thread walking a whole row.
+// loads in flight instead of one thread walking a whole row. One or two
+// right-hand sides (blockIdx.y).
 // y[i1, i2] = sum_k M1^{-1}[i1, k] b[k, i2]
 __global__ void __launch_bounds__(256)
-k_mass1(const double *__restrict__ Minv1, const double *__restrict__ b, int nd1, int nd2,
-        double *__restrict__ y) {
+k_mass1(const double *__restrict__ Minv1, const double *__restrict__ b0,
+        double *__restrict__ y0, const double *__restrict__ b1, double *__restrict__ y1,
+        int nd1, int nd2) {
+    const double *__restrict__ b = blockIdx.y ? b1 : b0;
+    double *__restrict__ y = blockIdx.y ? y1 : y0;
     const int t = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (t >= nd1 * nd2) return;
     const int i1 = t % nd1, i2 = t / nd1;
@@ -284,8 +332,11 @@ k_mass1(const double *__restrict__ Minv1, const double *__restrict__ b, int nd1,
 
 // out[i1, i2] = sum_k y[i1, k] M2^{-1}[k, i2]
 __global__ void __launch_bounds__(256)
-k_mass2(const double *__restrict__ Minv2, const double *__restrict__ y, int nd1, int nd2,
-        double *__restrict__ out) {
+k_mass2(const double *__restrict__ Minv2, const double *__restrict__ y0,
+        double *__restrict__ out0, const double *__restrict__ y1, double *__restrict__ out1,
+        int nd1, int nd2) {
+    const double *__restrict__ y = blockIdx.y ? y1 : y0;
+    double *__restrict__ out = blockIdx.y ? out1 : out0;
     const int t = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (t >= nd1 * nd2) return;
     const int i1 = t % nd1, i2 = t / nd1;
@@ -296,45 +347,60 @@ k_mass2(const double *__restrict__ Minv2, const double *__restrict__ y, int nd1,
     if (lane == 0) out[t] = s;
 }
 
-// One warp per element (four per block): f at the nq x nq Gauss points (lane
-// l takes points l and l + 32), then r-local (mode 0) or the entropy partial
-// (mode 1). The field is evaluated in tensor-product form, f = sum_b p2_b
-// (sum_a c_ab p1_a), and a point's nine contributions are h p1_a p2_b with
-// h = integrand * w_q * |e|; nine threads then add the points in point order
-// (fixed, deterministic).
-#define ELEM_PER_BLOCK 4
-__global__ void __launch_bounds__(32 * ELEM_PER_BLOCK)
-k_elem(const double *__restrict__ fc, int n1, int n2, int nd1, int nq,
+// Element quadrature for r-local (mode 0, functions.jl:158-179) or the entropy
+// partial (mode 1, functions.jl:137-155). One thread per (element, Gauss row
+// q1): nq threads per element and 128 / nq elements per block, so the lanes
+// stay busy for any nq. GB300 issues FP64 at 1/64 of the FP32 rate and these
+// kernels are FP64-issue bound, so the tensor-product form is used throughout:
+//   g_b(q1)      = sum_a c_ab p1_a(q1)                 (once per row)
+//   f(q1, q2)    = sum_b g_b(q1) p2_b(q2)
+//   H_b(q1)      = sum_q2 h(q1, q2) p2_b(q2),  h = integrand * w_q * |e|
+//   r_ab         = sum_q1 p1_a(q1) H_b(q1)             (rows added in order)
+// about 400 FP64 operations and nq^2 logarithms per element instead of ~30 per
+// Gauss point plus the logarithm. Fixed summation order: deterministic. Two jobs
+// may share a launch (blockIdx.y selects), e.g. r at v_mid and S at v_in.
+struct co_elem_job {
+    const double *fc;   // spline coefficients (n_dofs)
+    int mode;           // 0: r-local -> out[e][9]; 1: entropy partial -> out[e]
+    double *out;
+};
+
+#define ELEM_THREADS 128
+__global__ void __launch_bounds__(ELEM_THREADS)
+k_elem(co_elem_job j0, co_elem_job j1, int n1, int n2, int nd1, int nq,
        const double *__restrict__ Tq1, const double *__restrict__ Tq2,
        const double *__restrict__ qw, const double *__restrict__ bp1,
-       const double *__restrict__ bp2, int logsq, int mode, double *__restrict__ E,
-       double *__restrict__ Ep) {
-    __shared__ double contrib[ELEM_PER_BLOCK][64 * 9];
-    __shared__ double cs[ELEM_PER_BLOCK][9];
-    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
-    const int e = blockIdx.x * ELEM_PER_BLOCK + wl;
-    const bool live = e < n1 * n2;
-    const int i = live ? e % n1 : 0, j = live ? e / n1 : 0;
-    if (live && lane < 9) cs[wl][lane] = fc[(i + lane % 3) + (j + lane / 3) * nd1];
-    __syncwarp();
-    const int nqq = nq * nq;
-    if (live) {
+       const double *__restrict__ bp2, int logsq) {
+    __shared__ double part[ELEM_THREADS * 9];
+    const co_elem_job jb = blockIdx.y ? j1 : j0;
+    const int mode = jb.mode;
+    const int epb = ELEM_THREADS / nq;
+    const int t = threadIdx.x, el = t / nq, q1 = t - el * nq;
+    const int e = blockIdx.x * epb + el;
+    const int n_el = n1 * n2;
+    if (el < epb && e < n_el) {
+        const int i = e % n1, j = e / n1;
         const double jac = (bp1[i + 1] - bp1[i]) * (bp2[j + 1] - bp2[j]);
-        for (int t = lane; t < nqq; t += 32) {
-            const int q1 = t % nq, q2 = t / nq;
-            double p1[3], p2[3];
-            for (int a = 0; a < 3; a++) {
-                p1[a] = Tq1[((size_t)i * 3 + a) * nq + q1];
-                p2[a] = Tq2[((size_t)j * 3 + a) * nq + q2];
-            }
-            double f = 0.0;
-            for (int bb = 0; bb < 3; bb++) {
-                double g = cs[wl][3 * bb] * p1[0];
-                g = fma(cs[wl][3 * bb + 1], p1[1], g);
-                g = fma(cs[wl][3 * bb + 2], p1[2], g);
-                f = fma(g, p2[bb], f);
-            }
-            const double wj = qw[q1] * qw[q2] * jac;
+        const double *fc = jb.fc;
+        double p1[3], g[3];
+#pragma unroll
+        for (int a = 0; a < 3; a++) p1[a] = Tq1[((size_t)i * 3 + a) * nq + q1];
+#pragma unroll
+        for (int bb = 0; bb < 3; bb++) {
+            const double *cr = fc + i + (j + bb) * nd1;
+            double v = cr[0] * p1[0];
+            v = fma(cr[1], p1[1], v);
+            g[bb] = fma(cr[2], p1[2], v);
+        }
+        const double wq1 = qw[q1];
+        double H0 = 0.0, H1 = 0.0, H2 = 0.0, sv = 0.0;
+        const double *T2 = Tq2 + (size_t)j * 3 * nq;
+        for (int q2 = 0; q2 < nq; q2++) {
+            const double p20 = T2[q2], p21 = T2[nq + q2], p22 = T2[2 * nq + q2];
+            double f = g[0] * p20;
+            f = fma(g[1], p21, f);
+            f = fma(g[2], p22, f);
+            const double wj = wq1 * qw[q2] * jac;
             if (mode == 0) {
                 double integrand;
                 if (logsq)
@@ -342,36 +408,37 @@ k_elem(const double *__restrict__ fc, int n1, int n2, int nd1, int nq,
                 else
                     integrand = f > 1e-30 ? (1 + log(f)) : 0.0;
                 const double h = integrand * wj;
-                const double h0 = h * p1[0], h1 = h * p1[1], h2 = h * p1[2];
-                double *o = &contrib[wl][t * 9];
-                for (int bb = 0; bb < 3; bb++) {
-                    o[3 * bb] = h0 * p2[bb];
-                    o[3 * bb + 1] = h1 * p2[bb];
-                    o[3 * bb + 2] = h2 * p2[bb];
-                }
-            } else {
-                double sv = 0.0;
-                if (logsq) {
-                    if (f * f > 1e-60) sv = -(f * 0.5 * log(f * f) * wj);
-                } else if (f > 1e-30) {
-                    sv = -(f * log(f) * wj);
-                }
-                contrib[wl][t] = sv;
+                H0 = fma(h, p20, H0);
+                H1 = fma(h, p21, H1);
+                H2 = fma(h, p22, H2);
+            } else if (logsq) {
+                if (f * f > 1e-60) sv += -(f * 0.5 * log(f * f) * wj);
+            } else if (f > 1e-30) {
+                sv += -(f * log(f) * wj);
             }
         }
-    }
-    __syncwarp();
-    if (!live) return;
-    if (mode == 0) {
-        if (lane < 9) {
-            double sum = 0.0;
-            for (int q = 0; q < nqq; q++) sum += contrib[wl][q * 9 + lane];
-            E[(size_t)e * 9 + lane] = sum;
+        double *o = part + (size_t)t * 9;
+        if (mode == 0) {
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                o[a] = p1[a] * H0;
+                o[3 + a] = p1[a] * H1;
+                o[6 + a] = p1[a] * H2;
+            }
+        } else {
+            o[0] = sv;
         }
-    } else if (lane == 0) {
-        double sum = 0.0;
-        for (int q = 0; q < nqq; q++) sum += contrib[wl][q];
-        Ep[e] = sum;
+    }
+    __syncthreads();
+    const int ncomp = mode == 0 ? 9 : 1;
+    for (int k = t; k < epb * ncomp; k += blockDim.x) {
+        const int el2 = k / ncomp, comp = k - el2 * ncomp;
+        const int e2 = blockIdx.x * epb + el2;
+        if (e2 >= n_el) continue;
+        const double *src = part + (size_t)el2 * nq * 9 + comp;
+        double s = 0.0;
+        for (int r = 0; r < nq; r++) s += src[r * 9];
+        jb.out[(size_t)e2 * ncomp + comp] = s;
     }
 }
 
@@ -489,8 +556,8 @@ k_sum_to(const double *__restrict__ Ep, int n, double *__restrict__ out) {
 __global__ void __launch_bounds__(CO_RED_THREADS)
 k_grad_L(const double *__restrict__ x, int N, const int *__restrict__ cell,
          const double *__restrict__ xi, const double *__restrict__ Lc, int n1, int nd1,
-         const double *__restrict__ bp1, const double *__restrict__ bp2,
-         const double *__restrict__ C1, const double *__restrict__ C2,
+         const double *__restrict__ IH1, const double *__restrict__ IH2,
+         const double *__restrict__ P1, const double *__restrict__ P2,
          double *__restrict__ G, const double *__restrict__ w, double *__restrict__ dS,
          const double *__restrict__ dv, double *__restrict__ red) {
     __shared__ double sh[32];
@@ -500,21 +567,26 @@ k_grad_L(const double *__restrict__ x, int N, const int *__restrict__ cell,
         double acc1 = 0.0, acc2 = 0.0;
         if (c >= 0) {
             int i = c % n1, j = c / n1;
-            double h1 = bp1[i + 1] - bp1[i], h2 = bp2[j + 1] - bp2[j];
-            double ih1 = 1.0 / h1, ih2 = 1.0 / h2;
-            double B1[3], dB1[3], B2[3], dB2[3], p1[3], dp1[3], p2[3], dp2[3];
-            bern2(xi[a], B1, dB1);
-            bern2(xi[N + a], B2, dB2);
-            extract3(C1 + 9 * i, B1, p1);
-            extract3(C1 + 9 * i, dB1, dp1);
-            extract3(C2 + 9 * j, B2, p2);
-            extract3(C2 + 9 * j, dB2, dp2);
-            for (int b = 0; b < 3; b++)
-                for (int q = 0; q < 3; q++) {
-                    double Lv = Lc[(i + q) + (j + b) * nd1];
-                    acc1 += Lv * (dp1[q] * p2[b]) * ih1;
-                    acc2 += Lv * (p1[q] * dp2[b]) * ih2;
-                }
+            double p1[3], dp1[3], p2[3], dp2[3];
+            basis_mono(P1 + 12 * i, xi[a], p1, dp1);
+            basis_mono(P2 + 12 * j, xi[N + a], p2, dp2);
+            // tensor-product form: dL/dx1 = (1/h1) sum_b p2_b sum_q L_qb dp1_q and
+            // dL/dx2 = (1/h2) sum_b dp2_b sum_q L_qb p1_q (26 FP64 operations
+            // instead of 54 for the nine terms one by one)
+            double t1 = 0.0, t2 = 0.0;
+#pragma unroll
+            for (int b = 0; b < 3; b++) {
+                const double *Lr = Lc + i + (j + b) * nd1;
+                double s1 = Lr[0] * dp1[0], s2 = Lr[0] * p1[0];
+                s1 = fma(Lr[1], dp1[1], s1);
+                s2 = fma(Lr[1], p1[1], s2);
+                s1 = fma(Lr[2], dp1[2], s1);
+                s2 = fma(Lr[2], p1[2], s2);
+                t1 = fma(s1, p2[b], t1);
+                t2 = fma(s2, dp2[b], t2);
+            }
+            acc1 = t1 * IH1[i];
+            acc2 = t2 * IH2[j];
         }
         G[a] = acc1;
         G[N + a] = acc2;
@@ -698,78 +770,165 @@ __global__ void k_features_res(int N, const double *__restrict__ r, double inv_d
 
 // ---------------------------------------------------------------- host side
 
-int co_mid_dv(co_ctx *c, const double *vin, const double *v0, int N) {
-    if (N == 0) return CO_OK;
-    k_mid_dv<<<co_cdiv(2LL * N, 256), 256, 0, c->stream>>>(vin, v0, c->mb.vmid, c->mb.dv, 2 * N);
-    c->launches++;
-    CO_CK(cudaGetLastError());
+// set 0: the context's primary sort/projection buffers
+static co_sortset primary_set(co_ctx *c) {
+    co_bufs &b = c->mb;
+    co_sortset s;
+    s.cell = b.cell;
+    s.inv = b.inv;
+    s.perm = b.perm;
+    s.scell = b.scell;
+    s.hist = b.hist;
+    s.hoff = b.hoff;
+    s.count = b.count;
+    s.cstart = b.cstart;
+    s.xi = b.xi;
+    s.sw = b.sw;
+    s.sphi = b.sphi;
+    s.bS = c->bS;
+    s.b = c->b;
+    s.y = c->y;
+    return s;
+}
+
+void co_sortset_free(co_ctx *c) {
+    co_sortset &g = c->gs;
+    void *p[] = {g.cell, g.inv, g.perm, g.scell, g.hist, g.hoff, g.count, g.cstart,
+                 g.xi, g.sw, g.sphi, g.bS, g.b, g.y};
+    for (void *q : p)
+        if (q) cudaFree(q);
+    memset(&g, 0, sizeof(g));
+    c->gs_cap = 0;
+}
+
+// set 1 at the context's marker capacity
+static int ensure_gs(co_ctx *c) {
+    if (c->gs_cap == c->mb.cap && c->gs.cell) return CO_OK;
+    co_sortset_free(c);
+    co_sortset &g = c->gs;
+    const size_t cap = (size_t)c->mb.cap, nch = (size_t)c->mb.nchunk_cap, ne = c->n_el;
+    bool ok = cudaMalloc(&g.cell, sizeof(int) * cap) == cudaSuccess &&
+              cudaMalloc(&g.inv, sizeof(int) * cap) == cudaSuccess &&
+              cudaMalloc(&g.perm, sizeof(int) * cap) == cudaSuccess &&
+              cudaMalloc(&g.scell, sizeof(int) * cap) == cudaSuccess &&
+              cudaMalloc(&g.hist, sizeof(int) * nch * ne) == cudaSuccess &&
+              cudaMalloc(&g.hoff, sizeof(int) * nch * ne) == cudaSuccess &&
+              cudaMalloc(&g.count, sizeof(int) * ne) == cudaSuccess &&
+              cudaMalloc(&g.cstart, sizeof(int) * (ne + 1)) == cudaSuccess &&
+              cudaMalloc(&g.xi, sizeof(double) * 2 * cap) == cudaSuccess &&
+              cudaMalloc(&g.sw, sizeof(double) * cap) == cudaSuccess &&
+              cudaMalloc(&g.sphi, sizeof(double) * 6 * cap) == cudaSuccess &&
+              cudaMalloc(&g.bS, sizeof(double) * 9 * ne) == cudaSuccess &&
+              cudaMalloc(&g.b, sizeof(double) * c->n_dofs) == cudaSuccess &&
+              cudaMalloc(&g.y, sizeof(double) * c->n_dofs) == cudaSuccess;
+    if (!ok) {
+        co_sortset_free(c);
+        return CO_ERR_NOMEM;
+    }
+    c->gs_cap = c->mb.cap;
     return CO_OK;
 }
 
-// locate + stable sort of markers x (N). Results: mb.cell, mb.xi, mb.perm,
-// mb.inv, mb.scell, mb.sw, mb.sphi, cstart (M_in = cstart[n_el] on device).
-int co_sort_markers(co_ctx *c, const double *x, int N) {
+// locate + stable sort of one or two marker sets (jobs j0 -> set 0, j1 -> set 1)
+static int sort_sets(co_ctx *c, const co_locate_job &j0, const co_locate_job &j1, int nsets,
+                     int N) {
     co_bufs &b = c->mb;
+    const co_sortset s0 = primary_set(c), s1 = nsets > 1 ? c->gs : s0;
     int nchunk = co_cdiv(N, CO_CHUNK);
     if (nchunk == 0) nchunk = 1;
     size_t sm = sizeof(int) * (size_t)c->n_el;
     if (N > 0) {
-        k_locate_hist<<<nchunk, CO_CHUNK, sm, c->stream>>>(x, N, c->bp1, c->n1, c->bp2, c->n2,
-                                                          b.cell, b.xi, b.hist, c->n_el);
+        k_locate_hist<<<dim3(nchunk, nsets), CO_CHUNK, sm, c->stream>>>(
+            j0, j1, N, c->bp1, c->n1, c->bp2, c->n2, c->ih1, c->ih2, c->n_el);
         c->launches++;
     } else {
-        CO_CK(cudaMemsetAsync(b.hist, 0, sizeof(int) * c->n_el, c->stream));
+        CO_CK(cudaMemsetAsync(s0.hist, 0, sizeof(int) * c->n_el, c->stream));
+        if (nsets > 1) CO_CK(cudaMemsetAsync(s1.hist, 0, sizeof(int) * c->n_el, c->stream));
     }
-    k_cellcount<<<co_cdiv(c->n_el, 256), 256, 0, c->stream>>>(b.hist, N > 0 ? nchunk : 1,
-                                                              c->n_el, b.hoff, b.count);
-    k_cellscan<<<1, 1024, 0, c->stream>>>(b.count, c->n_el, b.cstart);
+    k_cellcount<<<dim3(co_cdiv(c->n_el, 256), nsets), 256, 0, c->stream>>>(
+        s0, s1, N > 0 ? nchunk : 1, c->n_el);
+    k_cellscan<<<dim3(1, nsets), 1024, 0, c->stream>>>(s0, s1, c->n_el);
     c->launches += 2;
     if (N > 0) {
-        k_perm<<<nchunk, CO_CHUNK, sm, c->stream>>>(b.cell, N, b.hoff, b.cstart, c->n_el, c->n1,
-                                                   b.w, b.xi, c->C1, c->C2, b.perm, b.inv,
-                                                   b.scell, b.sw, b.sphi);
+        k_perm<<<dim3(nchunk, nsets), CO_CHUNK, sm, c->stream>>>(s0, s1, N, c->n_el, c->n1,
+                                                                 b.w, c->P1, c->P2);
         c->launches++;
     }
+    CO_CK(cudaGetLastError());
+    return CO_OK;
+}
+
+// locate + stable sort of markers x (N) into set 0. Results: mb.cell, mb.xi,
+// mb.perm, mb.inv, mb.scell, mb.sw, mb.sphi, cstart (M_in = cstart[n_el]).
+int co_sort_markers(co_ctx *c, const double *x, int N) {
+    co_bufs &b = c->mb;
+    co_locate_job j = {x, nullptr, nullptr, nullptr, b.cell, b.xi, b.hist};
+    return sort_sets(c, j, j, 1, N);
+}
+
+int co_sort_mid(co_ctx *c, const double *vin, const double *v0, int N, int two) {
+    co_bufs &b = c->mb;
+    int rc;
+    if (two && (rc = ensure_gs(c))) return rc;
+    co_locate_job j0 = {vin, v0, b.vmid, b.dv, b.cell, b.xi, b.hist};
+    co_locate_job j1 = j0;
+    if (two) j1 = {vin, nullptr, nullptr, nullptr, c->gs.cell, c->gs.xi, c->gs.hist};
+    return sort_sets(c, j0, j1, two ? 2 : 1, N);
+}
+
+static int mass_solve_two(co_ctx *c, const double *r0, double *y0, double *o0,
+                          const double *r1, double *y1, double *o1, int nsets) {
+    int n = c->n_dofs;
+    // one warp per output, eight per block
+    k_mass1<<<dim3(co_cdiv(n, 8), nsets), 256, 0, c->stream>>>(c->Minv1, r0, y0, r1, y1,
+                                                                c->nd1, c->nd2);
+    k_mass2<<<dim3(co_cdiv(n, 8), nsets), 256, 0, c->stream>>>(c->Minv2, y0, o0, y1, o1,
+                                                                c->nd1, c->nd2);
+    c->launches += 2;
     CO_CK(cudaGetLastError());
     return CO_OK;
 }
 
 int co_mass_solve_dev(co_ctx *c, const double *rhs, double *out) {
-    int n = c->n_dofs;
-    // one warp per output, eight per block
-    k_mass1<<<co_cdiv(n, 8), 256, 0, c->stream>>>(c->Minv1, rhs, c->nd1, c->nd2, c->y);
-    k_mass2<<<co_cdiv(n, 8), 256, 0, c->stream>>>(c->Minv2, c->y, c->nd1, c->nd2, out);
+    return mass_solve_two(c, rhs, c->y, out, rhs, c->y, out, 1);
+}
+
+int co_project_two(co_ctx *c, double *f0, double *f1, int two) {
+    const int nsets = two ? 2 : 1;
+    const co_sortset s0 = primary_set(c), s1 = two ? c->gs : s0;
+    k_cellsum<<<dim3(c->n_el, nsets), 128, 0, c->stream>>>(s0, s1, c->n_el);
+    k_dofgather<<<dim3(co_cdiv(c->n_dofs, 128), nsets), 128, 0, c->stream>>>(
+        s0.bS, s0.b, s1.bS, s1.b, c->n1, c->n2, c->nd1, c->nd2);
     c->launches += 2;
     CO_CK(cudaGetLastError());
-    return CO_OK;
+    return mass_solve_two(c, s0.b, s0.y, f0, s1.b, s1.y, two ? f1 : f0, nsets);
 }
 
 // after co_sort_markers: b = scatter, f = M^{-1} b
-int co_project_sorted(co_ctx *c, double *f_out) {
-    k_cellsum<<<c->n_el, 128, 0, c->stream>>>(c->mb.cstart, c->mb.sw, c->mb.sphi,
-                                                          c->n_el, c->bS);
-    k_dofgather<<<co_cdiv(c->n_dofs, 128), 128, 0, c->stream>>>(c->bS, c->n1, c->n2, c->nd1,
-                                                                c->nd2, c->b);
-    c->launches += 2;
-    CO_CK(cudaGetLastError());
-    return co_mass_solve_dev(c, c->b, f_out);
-}
+int co_project_sorted(co_ctx *c, double *f_out) { return co_project_two(c, f_out, f_out, 0); }
 
-int co_compute_r_dev(co_ctx *c, const double *f, double *r) {
-    k_elem<<<co_cdiv(c->n_el, ELEM_PER_BLOCK), 32 * ELEM_PER_BLOCK, 0, c->stream>>>(
-        f, c->n1, c->n2, c->nd1, c->nq, c->Tq1, c->Tq2, c->qw, c->bp1, c->bp2,
-        (c->flags & CO_FLAG_LOGSQ) ? 1 : 0, 0, c->E, nullptr);
-    k_dofgather<<<co_cdiv(c->n_dofs, 128), 128, 0, c->stream>>>(c->E, c->n1, c->n2, c->nd1,
-                                                                c->nd2, r);
+int co_r_and_entropy_dev(co_ctx *c, const double *f, double *r, const double *fS) {
+    co_elem_job jr = {f, 0, c->E};
+    co_elem_job js = {fS, 1, c->Ep};
+    k_elem<<<dim3(co_cdiv(c->n_el, ELEM_THREADS / c->nq), fS ? 2 : 1), ELEM_THREADS, 0,
+             c->stream>>>(jr, js, c->n1, c->n2, c->nd1, c->nq, c->Tq1, c->Tq2, c->qw, c->bp1,
+                          c->bp2, (c->flags & CO_FLAG_LOGSQ) ? 1 : 0);
+    k_dofgather<<<dim3(co_cdiv(c->n_dofs, 128), 1), 128, 0, c->stream>>>(
+        c->E, r, c->E, r, c->n1, c->n2, c->nd1, c->nd2);
     c->launches += 2;
     CO_CK(cudaGetLastError());
     return CO_OK;
 }
 
+int co_compute_r_dev(co_ctx *c, const double *f, double *r) {
+    return co_r_and_entropy_dev(c, f, r, nullptr);
+}
+
 int co_entropy_parts_dev(co_ctx *c, const double *f) {
-    k_elem<<<co_cdiv(c->n_el, ELEM_PER_BLOCK), 32 * ELEM_PER_BLOCK, 0, c->stream>>>(
-        f, c->n1, c->n2, c->nd1, c->nq, c->Tq1, c->Tq2, c->qw, c->bp1, c->bp2,
-        (c->flags & CO_FLAG_LOGSQ) ? 1 : 0, 1, nullptr, c->Ep);
+    co_elem_job js = {f, 1, c->Ep};
+    k_elem<<<dim3(co_cdiv(c->n_el, ELEM_THREADS / c->nq), 1), ELEM_THREADS, 0, c->stream>>>(
+        js, js, c->n1, c->n2, c->nd1, c->nq, c->Tq1, c->Tq2, c->qw, c->bp1, c->bp2,
+        (c->flags & CO_FLAG_LOGSQ) ? 1 : 0);
     c->launches++;
     CO_CK(cudaGetLastError());
     return CO_OK;
@@ -812,7 +971,7 @@ int co_grad_L_dev(co_ctx *c, const double *x, int N, const double *L, double *G,
                   const double *w, double *dS, const double *dv, double *red) {
     if (N == 0) return CO_OK;
     k_grad_L<<<red_grid(c, N), CO_RED_THREADS, 0, c->stream>>>(
-        x, N, c->mb.cell, c->mb.xi, L, c->n1, c->nd1, c->bp1, c->bp2, c->C1, c->C2, G, w, dS, dv,
+        x, N, c->mb.cell, c->mb.xi, L, c->n1, c->nd1, c->ih1, c->ih2, c->P1, c->P2, G, w, dS, dv,
         red);
     c->launches++;
     CO_CK(cudaGetLastError());
@@ -883,6 +1042,9 @@ int co_ensure_capacity(co_ctx *c, int N, int m) {
         if ((rc = grow(&b.hoff, (size_t)nchunk * c->n_el))) return rc;
         b.nchunk_cap = nchunk;
         b.cap = cap;
+        // set 1 is allocated with set 0, never on first use: the Picard maps
+        // that use it are captured into CUDA graphs, where no allocation may run
+        if ((rc = ensure_gs(c))) return rc;
         double **lazy[] = {&b.Gk, &b.Phi, &b.Adef, &b.aa, &b.pc};  // re-created at the new size on use
         for (double **q : lazy) {
             if (*q) cudaFree(*q);

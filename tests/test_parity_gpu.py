@@ -498,3 +498,39 @@ def test_launch_counter_moves(built_lib, collops_mod):
     collops_mod.l2_project_gpu(ws, f, v, w)
     assert ws.launch_count() > n0
     ws.close()
+
+
+@pytest.mark.parametrize("precision,outer_m,precond", [("fp64", 0, 0), ("mixed_ds", 5, 1)])
+def test_step_defect_device_loop_matches_host_loop(built_lib, collops_mod, monkeypatch,
+                                                   precision, outer_m, precond):
+    """The inner Anderson loop of step_defect! runs on the device (one CUDA graph
+    whose body repeats under a conditional node) unless COLLOPS_INNER_LOOP=host
+    selects the host-driven loop. Both launch the same kernels on the same data
+    in the same order, so the steps agree bit for bit, with the same outer and
+    inner iteration counts."""
+    bp = uniform_bp(-6.0, 6.0, 16)
+    v, w = gaussian_markers(2048, 1.0, 0.5, seed=5)
+    ws = collops_mod.build_workspace(collops_mod.SimParameters(bp1=bp, bp2=bp))
+    f = np.zeros(ws.n_dofs)
+    collops_mod.l2_project_gpu(ws, f, v, w)
+    S0 = collops_mod.compute_entropy_gpu(ws, f)
+    dt = 0.02
+    v1 = np.zeros((2048, 2), order="F")
+    collops_mod.predictor(ws, v1, v, w, dt)
+    out = {}
+    for mode in ("device", "host"):
+        if mode == "host":
+            monkeypatch.setenv("COLLOPS_INNER_LOOP", "host")
+        else:
+            monkeypatch.delenv("COLLOPS_INNER_LOOP", raising=False)
+        x = np.array(v1, order="F", copy=True)
+        info = collops_mod.step_defect(ws, x, v, w, S0, dt, m=8, tol=1e-12, abs_floor=0.0,
+                                       damping=0.7, max_iter=200,
+                                       metric64=precision == "fp64", precision=precision,
+                                       outer_m=outer_m, precond=precond)
+        out[mode] = (x, info)
+    ws.close()
+    (xd, infod), (xh, infoh) = out["device"], out["host"]
+    print(f"device {infod} host {infoh}")
+    assert infod[0] == infoh[0] and infod[2] == infoh[2] and infod[1] == infoh[1]
+    assert np.array_equal(xd, xh)
