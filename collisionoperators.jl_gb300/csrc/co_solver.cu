@@ -403,7 +403,10 @@ k_anderson_cols(int n2, co_solver_state *st, const double *__restrict__ r,
                 double *__restrict__ red) {
     if (st->done || st->path != 1) return;
     const int slot = st->slot - 1, hist = st->history;
+    // the window loops run to CO_MAX_M, unrolled with a guard, so that pa, pb
+    // stay in registers (a runtime bound would put them in local memory)
     double pa[CO_MAX_M], pb[CO_MAX_M];
+#pragma unroll
     for (int j = 0; j < CO_MAX_M; j++) pa[j] = pb[j] = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
         double ri = r[i], gi = Gv[i];
@@ -413,17 +416,22 @@ k_anderson_cols(int n2, co_solver_state *st, const double *__restrict__ r,
         dG[(size_t)slot * ldF + i] = Gd;
         rp[i] = ri;
         Gp[i] = gi;
-        for (int j = 0; j < hist; j++) {
-            double fj = j == slot ? F : dF[(size_t)j * ldF + i];
-            pa[j] += F * fj;
-            pb[j] += fj * ri;
+#pragma unroll
+        for (int j = 0; j < CO_MAX_M; j++) {
+            if (j < hist) {
+                double fj = j == slot ? F : dF[(size_t)j * ldF + i];
+                pa[j] += F * fj;
+                pb[j] += fj * ri;
+            }
         }
     }
     // all 2*hist block sums at once: shuffle trees per warp, then warp partials
     // summed in warp order by one thread per value (fixed order, one barrier)
     __shared__ double wsum[CO_RED_THREADS / 32][2 * CO_MAX_M];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int j = 0; j < hist; j++) {
+#pragma unroll
+    for (int j = 0; j < CO_MAX_M; j++) {
+        if (j >= hist) break;
         double a = pa[j], b = pb[j];
         for (int o = 16; o > 0; o >>= 1) {
             a += __shfl_down_sync(0xffffffffu, a, o);
@@ -466,37 +474,87 @@ k_anderson_solve(const double *__restrict__ red, int nred, co_solver_state *st, 
         st->ATA[slot * CO_MAX_M + j] = dots[j];
         st->ATA[j * CO_MAX_M + slot] = dots[j];
     }
-    double A[CO_MAX_M * CO_MAX_M], b[CO_MAX_M];
-    for (int i = 0; i < h; i++) {
-        for (int j = 0; j < h; j++) A[i * h + j] = st->ATA[i * CO_MAX_M + j];
-        b[i] = dots[CO_MAX_M + i];
+    // LU with partial pivoting on the leading h x h block. Every loop runs to
+    // CO_MAX_M, unrolled with guards, and row swaps are predicated moves, so A
+    // and b live in registers; the operations on the h x h block and their
+    // order are those of the plain loops.
+    double A[CO_MAX_M][CO_MAX_M], b[CO_MAX_M];
+#pragma unroll
+    for (int i = 0; i < CO_MAX_M; i++) {
+#pragma unroll
+        for (int j = 0; j < CO_MAX_M; j++)
+            A[i][j] = (i < h && j < h) ? st->ATA[i * CO_MAX_M + j] : 0.0;
+        b[i] = i < h ? dots[CO_MAX_M + i] : 0.0;
     }
     double dm = 0.0;
-    for (int j = 0; j < h; j++) dm += A[j * h + j];
+#pragma unroll
+    for (int j = 0; j < CO_MAX_M; j++)
+        if (j < h) dm += A[j][j];
     dm /= h;
     double l2 = o.reg_factor * dm + 1e-30;
-    for (int j = 0; j < h; j++) A[j * h + j] += l2;
+#pragma unroll
+    for (int j = 0; j < CO_MAX_M; j++)
+        if (j < h) A[j][j] += l2;
     int piv[CO_MAX_M];
-    for (int k = 0; k < h; k++) {
+#pragma unroll
+    for (int k = 0; k < CO_MAX_M; k++) {
+        if (k >= h) continue;
         int p = k;
-        double mx = fabs(A[k * h + k]);
-        for (int i = k + 1; i < h; i++)
-            if (fabs(A[i * h + k]) > mx) { mx = fabs(A[i * h + k]); p = i; }
+        double mx = fabs(A[k][k]);
+#pragma unroll
+        for (int i = k + 1; i < CO_MAX_M; i++)
+            if (i < h && fabs(A[i][k]) > mx) {
+                mx = fabs(A[i][k]);
+                p = i;
+            }
         piv[k] = p;
-        if (p != k)
-            for (int j = 0; j < h; j++) { double t = A[k * h + j]; A[k * h + j] = A[p * h + j]; A[p * h + j] = t; }
-        for (int i = k + 1; i < h; i++) {
-            A[i * h + k] /= A[k * h + k];
-            for (int j = k + 1; j < h; j++) A[i * h + j] -= A[i * h + k] * A[k * h + j];
+#pragma unroll
+        for (int i = k + 1; i < CO_MAX_M; i++)
+            if (i == p)
+#pragma unroll
+                for (int j = 0; j < CO_MAX_M; j++) {
+                    double t = A[k][j];
+                    A[k][j] = A[i][j];
+                    A[i][j] = t;
+                }
+#pragma unroll
+        for (int i = k + 1; i < CO_MAX_M; i++) {
+            if (i < h) {
+                A[i][k] /= A[k][k];
+#pragma unroll
+                for (int j = k + 1; j < CO_MAX_M; j++)
+                    if (j < h) A[i][j] -= A[i][k] * A[k][j];
+            }
         }
     }
-    for (int k = 0; k < h; k++) if (piv[k] != k) { double t = b[k]; b[k] = b[piv[k]]; b[piv[k]] = t; }
-    for (int i = 0; i < h; i++) for (int j = 0; j < i; j++) b[i] -= A[i * h + j] * b[j];
-    for (int i = h - 1; i >= 0; i--) {
-        for (int j = i + 1; j < h; j++) b[i] -= A[i * h + j] * b[j];
-        b[i] /= A[i * h + i];
+#pragma unroll
+    for (int k = 0; k < CO_MAX_M; k++) {
+        if (k >= h) continue;
+#pragma unroll
+        for (int i = k + 1; i < CO_MAX_M; i++)
+            if (piv[k] == i) {
+                double t = b[k];
+                b[k] = b[i];
+                b[i] = t;
+            }
     }
-    for (int j = 0; j < h; j++) st->gamma[j] = b[j];
+#pragma unroll
+    for (int i = 0; i < CO_MAX_M; i++)
+#pragma unroll
+        for (int j = 0; j < i; j++)
+            if (i < h) b[i] -= A[i][j] * b[j];
+#pragma unroll
+    for (int i = CO_MAX_M - 1; i >= 0; i--) {
+        if (i < h) {
+#pragma unroll
+            for (int j = i + 1; j < CO_MAX_M; j++)
+                if (j < h) b[i] -= A[i][j] * b[j];
+            b[i] /= A[i][i];
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < CO_MAX_M; j++)
+        if (j < h) st->gamma[j] = b[j];
 }
 
 // v1 = damp (Gv - dG gamma) + (1 - damp) v_old (solver.jl:410-412)
@@ -507,10 +565,13 @@ __global__ void k_anderson_update(int n2, co_solver_state *st, double *__restric
     const int h = st->history;
     const double damp = st->damp;
     double gam[CO_MAX_M];
-    for (int j = 0; j < h; j++) gam[j] = st->gamma[j];
+#pragma unroll
+    for (int j = 0; j < CO_MAX_M; j++) gam[j] = j < h ? st->gamma[j] : 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
         double s = Gv[i];
-        for (int j = 0; j < h; j++) s += -1.0 * dG[(size_t)j * ldF + i] * gam[j];
+#pragma unroll
+        for (int j = 0; j < CO_MAX_M; j++)
+            if (j < h) s += -1.0 * dG[(size_t)j * ldF + i] * gam[j];
         v1[i] = damp * s + (1 - damp) * v1[i];
     }
 }
