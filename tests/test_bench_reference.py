@@ -26,3 +26,8 @@ def test_reference_arm_json_line(oracle_mod):
     assert len(line["map_ms"]) == 2 and line["extrapolated"] is True
     assert abs(line["value"] - line["per_map_ms"] * line["maps_per_step"]) <= 0.1 * line["value"]
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
+    # `steps` is the fraction of a converged step the timed maps make up, so that
+    # ms_per_step x steps matches the timed region
+    assert line["maps_timed"] == 2
+    assert abs(line["steps"] - 2 / line["maps_per_step"]) < 1e-4
+    assert abs(line["ms_per_step"] * line["steps"] - sum(line["map_ms"])) <= 0.2 * sum(line["map_ms"])
