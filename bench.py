@@ -777,6 +777,9 @@ def main(argv=None):
                          "FP64_MAPS_PER_STEP)")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--N", type=int, default=None, help="override the marker count (tests)")
+    ap.add_argument("--seed", type=int, default=None,
+                    help="marker seed (default 42; other seeds give other trajectories of "
+                         "the same workload, for solver-setting comparisons)")
     ap.add_argument("--profile-maps", action="store_true",
                     help="run one Picard map per pair precision and exit (kernel captures)")
     ap.add_argument("--profile-maps-kinds", default="fp32,ds,fp64")
@@ -790,6 +793,9 @@ def main(argv=None):
     if args.N:
         cfg["N"] = args.N
         cfg["name"] = f"landau_n{args.N}_mesh64_dt0.02"
+    if args.seed is not None:
+        cfg["seed"] = args.seed
+        cfg["name"] += f"_seed{args.seed}"
     if args.profile_maps:
         run_profile_maps(args, cfg)
     elif args.impl == "reference":

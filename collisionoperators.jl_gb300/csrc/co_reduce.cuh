@@ -47,3 +47,35 @@ __device__ __forceinline__ double co_sum_partials(const double *red, int n, int 
     double s = co_strided_sum(red, threadIdx.x, n, blockDim.x, ncomp, comp, 0.0);
     return co_block_sum(s, sh);
 }
+
+// Sums each of the V values v[0..V) (V = 2, 4, 8 or 16) over the 32 lanes of a
+// warp by recursive halving: at each level a lane keeps the half of its values
+// that its lane bit selects and adds the partner's copy of that half; once one
+// value is left, plain butterfly levels finish the sum. The adds per lane are
+// V - 1 + (6 - log2 V) instead of 5 V for V shuffle trees, which matters at
+// GB300's FP64 rate. Returns the sum of value lane >> (5 - log2 V) (lanes that
+// differ only in the low bits hold the same sum). Fixed order, deterministic.
+// v is overwritten.
+template <int V>
+__device__ __forceinline__ double co_warp_sum(double (&v)[V], int lane) {
+    static_assert(V == 2 || V == 4 || V == 8 || V == 16, "V must be 2, 4, 8 or 16");
+    int bit = 16;
+#pragma unroll
+    for (int half = V / 2; half >= 1; half >>= 1, bit >>= 1) {
+        const bool up = (lane & bit) != 0;
+#pragma unroll
+        for (int i = 0; i < half; i++) {
+            const double send = up ? v[i] : v[half + i];
+            const double keep = up ? v[half + i] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, bit);
+        }
+    }
+    double s = v[0];
+#pragma unroll
+    for (; bit >= 1; bit >>= 1) s += __shfl_xor_sync(0xffffffffu, s, bit);
+    return s;
+}
+
+__device__ __forceinline__ double co_warp_sum16(double (&v)[16], int lane) {
+    return co_warp_sum<16>(v, lane);
+}

@@ -425,23 +425,21 @@ k_anderson_cols(int n2, co_solver_state *st, const double *__restrict__ r,
             }
         }
     }
-    // all 2*hist block sums at once: shuffle trees per warp, then warp partials
-    // summed in warp order by one thread per value (fixed order, one barrier)
+    // all 2*CO_MAX_M block sums at once: a recursive-halving warp reduction
+    // (16 FP64 adds per lane instead of 5 per value, which matters at GB300's
+    // FP64 rate), then warp partials summed in warp order by one thread per
+    // value (fixed order, one barrier)
+    static_assert(CO_MAX_M == 8, "k_anderson_cols reduces 2 x 8 values per lane");
     __shared__ double wsum[CO_RED_THREADS / 32][2 * CO_MAX_M];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    double v[2 * CO_MAX_M];
 #pragma unroll
     for (int j = 0; j < CO_MAX_M; j++) {
-        if (j >= hist) break;
-        double a = pa[j], b = pb[j];
-        for (int o = 16; o > 0; o >>= 1) {
-            a += __shfl_down_sync(0xffffffffu, a, o);
-            b += __shfl_down_sync(0xffffffffu, b, o);
-        }
-        if (lane == 0) {
-            wsum[warp][j] = a;
-            wsum[warp][CO_MAX_M + j] = b;
-        }
+        v[j] = pa[j];
+        v[CO_MAX_M + j] = pb[j];
     }
+    const double sj = co_warp_sum16(v, lane);   // value (lane >> 1)
+    if ((lane & 1) == 0) wsum[warp][lane >> 1] = sj;
     __syncthreads();
     const int t = threadIdx.x;
     if (t < 2 * CO_MAX_M && (t % CO_MAX_M) < hist) {
@@ -468,9 +466,15 @@ k_anderson_solve(const double *__restrict__ red, int nred, co_solver_state *st, 
             if (lane == 0) dots[col] = s;
         }
     }
+    // the cached Gram matrix through shared memory: the one thread that solves
+    // then reads it at shared-memory latency
+    __shared__ double sA[CO_MAX_M * CO_MAX_M];
+    for (int t = threadIdx.x; t < CO_MAX_M * CO_MAX_M; t += blockDim.x) sA[t] = st->ATA[t];
     __syncthreads();
     if (threadIdx.x != 0) return;
     for (int j = 0; j < h; j++) {
+        sA[slot * CO_MAX_M + j] = dots[j];
+        sA[j * CO_MAX_M + slot] = dots[j];
         st->ATA[slot * CO_MAX_M + j] = dots[j];
         st->ATA[j * CO_MAX_M + slot] = dots[j];
     }
@@ -483,7 +487,7 @@ k_anderson_solve(const double *__restrict__ red, int nred, co_solver_state *st, 
     for (int i = 0; i < CO_MAX_M; i++) {
 #pragma unroll
         for (int j = 0; j < CO_MAX_M; j++)
-            A[i][j] = (i < h && j < h) ? st->ATA[i * CO_MAX_M + j] : 0.0;
+            A[i][j] = (i < h && j < h) ? sA[i * CO_MAX_M + j] : 0.0;
         b[i] = i < h ? dots[CO_MAX_M + i] : 0.0;
     }
     double dm = 0.0;
@@ -607,6 +611,14 @@ static int red_blocks(co_ctx *c, int N) {
     int g = co_cdiv(N, CO_RED_THREADS);
     if (g > c->mb.red_cap) g = c->mb.red_cap;
     return g < 1 ? 1 : g;
+}
+
+// Grid of k_anderson_cols: two blocks per SM, each thread striding over several
+// elements, so the per-thread partial dot products cover several elements
+// before the (FP64) warp reduction
+static int window_blocks(co_ctx *c, int n2) {
+    int g = red_blocks(c, n2);
+    return g > 2 * c->nsm ? 2 * c->nsm : g;
 }
 
 int co_lb_fused(co_ctx *c, int N, double nu, double dt, double *Gv, const double *v0,
@@ -780,7 +792,7 @@ static int anderson_loop(co_ctx *c, const co_opts *o, int precision, int N, doub
                                                   b.rp, b.Gp, b.vbest);
         c->launches += 2;
         if (o->use_anderson) {
-            int ng = red_blocks(c, n2);
+            int ng = window_blocks(c, n2);
             k_anderson_cols<<<ng, CO_RED_THREADS, 0, c->stream>>>(n2, c->st, b.r, b.rp, b.Gv, b.Gp,
                                                                   b.dF, b.dG, ldF, b.red);
             k_anderson_solve<<<1, 256, 0, c->stream>>>(b.red, ng, c->st, d);
@@ -1251,7 +1263,7 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
         k_ctrl_inner<<<1, 256, 0, c->stream>>>(b.red, nred, c->st2, c->st, o->m, o->damping);
         k_plain_update<<<eg, 256, 0, c->stream>>>(n2, c->st2, 0, b.v1, mapv, res, b.rp, b.Gp,
                                                   b.vbest);
-        int ng = red_blocks(c, n2);
+        int ng = window_blocks(c, n2);
         k_anderson_cols<<<ng, CO_RED_THREADS, 0, c->stream>>>(n2, c->st2, res, b.rp, mapv,
                                                               b.Gp, b.dF, b.dG, ldF, b.red);
         k_anderson_solve<<<1, 256, 0, c->stream>>>(b.red, ng, c->st2, di);
@@ -1393,7 +1405,7 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
             k_aa_resid<<<eg, 256, 0, c->stream>>>(n2, c->st, b.v1, aa_vk, aa_u, aa_r);
             k_plain_update<<<eg, 256, 0, c->stream>>>(n2, c->st3, 0, aa_vk, aa_u, aa_r, aa_rp,
                                                       aa_Gp, b.vbest);
-            int ng = red_blocks(c, n2);
+            int ng = window_blocks(c, n2);
             k_anderson_cols<<<ng, CO_RED_THREADS, 0, c->stream>>>(n2, c->st3, aa_r, aa_rp, aa_u,
                                                                   aa_Gp, aa_dF, aa_dG, ld2, b.red);
             k_anderson_solve<<<1, 256, 0, c->stream>>>(b.red, ng, c->st3, di);
@@ -1694,7 +1706,7 @@ static int batch_iteration_impl(co_batch *B, const co_opts *o, const double *S0,
         k_ctrl1<<<1, 256, 0, cs>>>(b.red, nred[i], c->st, d);
         k_plain_update<<<eg, 256, 0, cs>>>(n2, c->st, o->exit_picard_step, b.v1, b.Gv, b.r, b.rp,
                                            b.Gp, b.vbest);
-        int ng = red_blocks(c, n2);
+        int ng = window_blocks(c, n2);
         k_anderson_cols<<<ng, CO_RED_THREADS, 0, cs>>>(n2, c->st, b.r, b.rp, b.Gv, b.Gp, b.dF,
                                                        b.dG, ldF, b.red);
         k_anderson_solve<<<1, 256, 0, cs>>>(b.red, ng, c->st, d);

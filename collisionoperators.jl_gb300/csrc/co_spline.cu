@@ -269,13 +269,17 @@ k_cellsum(co_sortset s0, co_sortset s1, int n_el) {
             acc[7] = fma(a1, b2, acc[7]);
             acc[8] = fma(a2, b2, acc[8]);
         }
+        // the nine lane sums by recursive halving (16 FP64 adds per lane instead
+        // of 45 for nine shuffle trees: at GB300's FP64 rate the trees cost more
+        // than the scatter itself)
+        double v[16];
 #pragma unroll
-        for (int j = 0; j < 9; j++)
-            for (int o = 16; o > 0; o >>= 1) acc[j] += __shfl_down_sync(0xffffffffu, acc[j], o);
+        for (int j = 0; j < 16; j++) v[j] = j < 9 ? acc[j] : 0.0;
+        const double sj = co_warp_sum16(v, lane);   // value (lane >> 1)
+        if ((lane & 1) == 0 && (lane >> 1) < 9) part[warp][lane >> 1] = sj;
+    } else if (lane < 9) {
+        part[warp][lane] = 0.0;
     }
-    if (lane == 0)
-#pragma unroll
-        for (int j = 0; j < 9; j++) part[warp][j] = acc[j];
     __syncthreads();
     if (threadIdx.x < 9) {
         const int j = threadIdx.x;
@@ -307,11 +311,13 @@ __global__ void k_dofgather(const double *__restrict__ src0, double *__restrict_
 }
 
 // The mass solve f = M1^{-1} B M2^{-1} (M = M2 (x) M1, first index fastest) as
-// two dense products with the 1D inverses. One warp per output: lane l adds the
-// terms k = l, l + 32, ... and a fixed shuffle tree sums the lanes, so the
-// dependent chain is ~nd/32 FMAs long instead of nd, and each warp keeps few
-// loads in flight instead of one thread walking a whole row. One or two
-// right-hand sides (blockIdx.y).
+// two dense products with the 1D inverses. One warp per eight consecutive
+// outputs i1 .. i1 + 7 of one column i2: lane l adds the terms k = l, l + 32,
+// ... of all eight (the eight inverse-matrix entries of a k are contiguous, the
+// right-hand-side entry is shared), then co_warp_sum<8> adds the lanes (9 FP64
+// adds per lane for the eight outputs instead of 5 per output). One or two
+// right-hand sides (blockIdx.y). Fixed order, deterministic.
+#define MASS_OUT 8
 // y[i1, i2] = sum_k M1^{-1}[i1, k] b[k, i2]
 __global__ void __launch_bounds__(256)
 k_mass1(const double *__restrict__ Minv1, const double *__restrict__ b0,
@@ -319,15 +325,25 @@ k_mass1(const double *__restrict__ Minv1, const double *__restrict__ b0,
         int nd1, int nd2) {
     const double *__restrict__ b = blockIdx.y ? b1 : b0;
     double *__restrict__ y = blockIdx.y ? y1 : y0;
-    const int t = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    if (t >= nd1 * nd2) return;
-    const int i1 = t % nd1, i2 = t / nd1;
+    const int ng1 = (nd1 + MASS_OUT - 1) / MASS_OUT;
+    const int wi = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (wi >= ng1 * nd2) return;
+    const int i1b = (wi % ng1) * MASS_OUT, i2 = wi / ng1;
     const double *col = b + (size_t)i2 * nd1;
-    double s = 0.0;
+    double s[MASS_OUT];
+#pragma unroll
+    for (int o = 0; o < MASS_OUT; o++) s[o] = 0.0;
     // Minv1 is exactly symmetric (symmetrised at set-up): row i1 read as column i1
-    for (int k = lane; k < nd1; k += 32) s = fma(Minv1[(size_t)k * nd1 + i1], col[k], s);
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if (lane == 0) y[t] = s;
+    for (int k = lane; k < nd1; k += 32) {
+        const double bk = col[k];
+        const double *mrow = Minv1 + (size_t)k * nd1;
+#pragma unroll
+        for (int o = 0; o < MASS_OUT; o++)
+            if (i1b + o < nd1) s[o] = fma(mrow[i1b + o], bk, s[o]);
+    }
+    const double r = co_warp_sum<MASS_OUT>(s, lane);   // output lane >> 2
+    const int o = lane >> 2;
+    if ((lane & 3) == 0 && i1b + o < nd1) y[(size_t)i2 * nd1 + i1b + o] = r;
 }
 
 // out[i1, i2] = sum_k y[i1, k] M2^{-1}[k, i2]
@@ -337,14 +353,23 @@ k_mass2(const double *__restrict__ Minv2, const double *__restrict__ y0,
         int nd1, int nd2) {
     const double *__restrict__ y = blockIdx.y ? y1 : y0;
     double *__restrict__ out = blockIdx.y ? out1 : out0;
-    const int t = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    if (t >= nd1 * nd2) return;
-    const int i1 = t % nd1, i2 = t / nd1;
-    double s = 0.0;
-    for (int k = lane; k < nd2; k += 32)
-        s = fma(y[(size_t)k * nd1 + i1], Minv2[(size_t)k * nd2 + i2], s);
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if (lane == 0) out[t] = s;
+    const int ng1 = (nd1 + MASS_OUT - 1) / MASS_OUT;
+    const int wi = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (wi >= ng1 * nd2) return;
+    const int i1b = (wi % ng1) * MASS_OUT, i2 = wi / ng1;
+    double s[MASS_OUT];
+#pragma unroll
+    for (int o = 0; o < MASS_OUT; o++) s[o] = 0.0;
+    for (int k = lane; k < nd2; k += 32) {
+        const double mk = Minv2[(size_t)k * nd2 + i2];
+        const double *yrow = y + (size_t)k * nd1;
+#pragma unroll
+        for (int o = 0; o < MASS_OUT; o++)
+            if (i1b + o < nd1) s[o] = fma(yrow[i1b + o], mk, s[o]);
+    }
+    const double r = co_warp_sum<MASS_OUT>(s, lane);   // output lane >> 2
+    const int o = lane >> 2;
+    if ((lane & 3) == 0 && i1b + o < nd1) out[(size_t)i2 * nd1 + i1b + o] = r;
 }
 
 // Element quadrature for r-local (mode 0, functions.jl:158-179) or the entropy
@@ -878,12 +903,12 @@ int co_sort_mid(co_ctx *c, const double *vin, const double *v0, int N, int two) 
 
 static int mass_solve_two(co_ctx *c, const double *r0, double *y0, double *o0,
                           const double *r1, double *y1, double *o1, int nsets) {
-    int n = c->n_dofs;
-    // one warp per output, eight per block
-    k_mass1<<<dim3(co_cdiv(n, 8), nsets), 256, 0, c->stream>>>(c->Minv1, r0, y0, r1, y1,
-                                                                c->nd1, c->nd2);
-    k_mass2<<<dim3(co_cdiv(n, 8), nsets), 256, 0, c->stream>>>(c->Minv2, y0, o0, y1, o1,
-                                                                c->nd1, c->nd2);
+    // one warp per MASS_OUT outputs of a column, eight warps per block
+    const int nw = co_cdiv(c->nd1, MASS_OUT) * c->nd2;
+    k_mass1<<<dim3(co_cdiv(nw, 8), nsets), 256, 0, c->stream>>>(c->Minv1, r0, y0, r1, y1,
+                                                                 c->nd1, c->nd2);
+    k_mass2<<<dim3(co_cdiv(nw, 8), nsets), 256, 0, c->stream>>>(c->Minv2, y0, o0, y1, o1,
+                                                                 c->nd1, c->nd2);
     c->launches += 2;
     CO_CK(cudaGetLastError());
     return CO_OK;
