@@ -297,7 +297,8 @@ def run_gpu(args, cfg):
     # dc_stag_window outer maps (Parameters.jl:89-91)
     dopt = co.CoDefectOpts(args.dc_eta, args.dc_max_inner, args.dc_stag_window,
                            args.dc_fp32_stall, 0, args.dc_outer_m, args.dc_precond,
-                           args.dc_metric_freeze, args.dc_fp32_window)
+                           args.dc_metric_freeze, args.dc_fp32_window, args.dc_cap_refresh,
+                           args.dc_cap_abort)
     dptr = C.byref(dopt) if args.solver == "defect" else None
 
     from collops import learned
@@ -762,6 +763,11 @@ def main(argv=None):
                          "residual (0: after the first map below the stall cut)")
     ap.add_argument("--dc-outer-m", type=int, default=5,
                     help="Anderson depth over the defect correction's outer iterates")
+    ap.add_argument("--dc-cap-refresh", type=int, default=0, choices=[0, 1],
+                    help="rebuild the FP32 metric after an inner solve that hit max_inner")
+    ap.add_argument("--dc-cap-abort", type=int, default=0,
+                    help="stagnation exit after this many FP64-stage outer maps in a row whose "
+                         "inner solve hit max_inner without a new best (0: off)")
     ap.add_argument("--dc-precond", type=int, default=0, choices=[0, 1, 2],
                     help="block-Newton preconditioner of the inner iteration")
     ap.add_argument("--no-accuracy", dest="accuracy", action="store_false")

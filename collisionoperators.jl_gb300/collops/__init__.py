@@ -78,7 +78,8 @@ class CoDefectOpts(C.Structure):
     """co_defect_opts of include/collops.h."""
     _fields_ = [("eta", C.c_double), ("max_inner", C.c_int), ("stag_window", C.c_int),
                 ("fp32_stall", C.c_double), ("metric64", C.c_int), ("outer_m", C.c_int),
-                ("precond", C.c_int), ("metric_freeze", C.c_double), ("fp32_window", C.c_int)]
+                ("precond", C.c_int), ("metric_freeze", C.c_double), ("fp32_window", C.c_int),
+                ("cap_refresh", C.c_int), ("cap_abort", C.c_int)]
 
 
 class CoNewtonOpts(C.Structure):

@@ -716,7 +716,7 @@ static int check_defect(const co_opts *o, const co_defect_opts *d) {
     int rc = check_opts(o);
     if (rc) return rc;
     if (!d || o->model != CO_MODEL_LANDAU || d->max_inner < 1 || d->stag_window < 1 ||
-        !(d->eta > 0))
+        !(d->eta > 0) || d->cap_abort < 0)
         return CO_ERR_ARG;
     return CO_OK;
 }

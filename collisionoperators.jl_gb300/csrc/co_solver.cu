@@ -1318,6 +1318,12 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
     };
     int aa_stage = -1;   // pair precision of the outer map the window was built on
     double first_outer = 0.0, prev_outer = 0.0;   // outer residuals (metric_freeze)
+    // capped inner solves (co_defect_opts.cap_refresh / cap_abort): whether the
+    // last inner solve hit max_inner, how many FP64-stage outer maps in a row
+    // ended in a capped inner solve without a new best outer residual, and that best
+    bool last_capped = false;
+    int capped_run = 0;
+    double best_outer64 = INFINITY;
     int k;
     for (k = 1; k <= max_outer; k++) {
         // ---- outer: G_eff(v_k), F (+ A), G(v_k), residual
@@ -1342,6 +1348,7 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
         // the FP32 metric is rebuilt while the previous outer residual is above
         // metric_freeze x the first (always at k = 1)
         const bool new_A = m64 || k == 1 || !(dopt->metric_freeze > 0.0) ||
+                           (dopt->cap_refresh && last_capped) ||
                            prev_outer >= dopt->metric_freeze * first_outer;
         if (!m64 && new_A)
             if ((rc = co_metric32(c, N))) return rc;
@@ -1390,6 +1397,12 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
             j = c->st_host->done ? ran : dopt->max_inner + 1;
         }
         total_inner += j > dopt->max_inner ? dopt->max_inner : j;
+        last_capped = j > dopt->max_inner;
+        if (stage == 0) {
+            const bool better = outer_nrm < best_outer64;
+            if (better) best_outer64 = outer_nrm;
+            capped_run = (last_capped && !better) ? capped_run + 1 : 0;
+        }
         if (co_verbose())
             fprintf(stderr, "    outer k=%d [%s]  |r|=%.6e  inner +%d%s\n", k,
                     stage == 1 ? "fp32" : ds ? "ds" : "fp64", outer_nrm,
@@ -1415,6 +1428,15 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
                                   c->stream));
         }
         stage = next_stage;
+        // cap_abort: the FP64-stage outer iteration has stopped improving while
+        // its inner solves no longer converge; leave through the stagnation exit
+        // (best iterate) at once instead of after the stagnation window
+        if (dopt->cap_abort > 0 && capped_run >= dopt->cap_abort) {
+            k_set_done<<<1, 32, 0, c->stream>>>(c->st, 2);
+            c->launches++;
+            c->st_host->done = 2;
+            break;
+        }
     }
     if (co_verbose())
         fprintf(stderr, "    outer k=%d  |r|=%.6e  [%s]\n", k > max_outer ? max_outer : k,

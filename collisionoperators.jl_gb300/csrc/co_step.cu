@@ -231,7 +231,7 @@ static int check_step_args(co_ctx *c, const co_opts *o, const co_defect_opts *d,
     if (o->precision < CO_PREC_FP64 || o->precision > CO_PREC_MIXED_DS) return CO_ERR_ARG;
     if (o->model == CO_MODEL_LB && o->precision != CO_PREC_FP64) return CO_ERR_ARG;
     if (d && (o->model != CO_MODEL_LANDAU || d->max_inner < 1 || d->stag_window < 1 ||
-              !(d->eta > 0)))
+              !(d->eta > 0) || d->cap_abort < 0))
         return CO_ERR_ARG;
     return CO_OK;
 }

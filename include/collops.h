@@ -188,6 +188,14 @@ typedef struct {
                        map cuts the residual by less than fp32_stall; W > 0
                        once W maps in a row brought no new best residual cut
                        by fp32_stall                                          */
+    int cap_refresh; /* with metric64 = 0: 1 rebuilds the FP32 metric at the
+                       outer map after an inner solve that hit max_inner, even
+                       past metric_freeze; 0 (the reference) does not         */
+    int cap_abort;   /* K > 0: leave through the stagnation exit (best
+                       iterate) once K FP64-stage outer maps in a row ended in
+                       an inner solve that hit max_inner without a new best
+                       outer residual; 0 (the reference) waits for the
+                       stagnation window                                      */
 } co_defect_opts;
 
 /* step_defect! (solver.jl:569-634): defect correction around a frozen
