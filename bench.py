@@ -568,6 +568,13 @@ def run_gpu(args, cfg):
                    "tol": cfg["tol"], "abs_floor": cfg["abs_floor"], "gonzalez": True,
                    "use_logsq": cfg["use_logsq"], "stag_window": cfg["stag_window"],
                    "stag_rel_tol": cfg["stag_rel_tol"], "dc_stag_window": args.dc_stag_window,
+                   "defect": {"eta": args.dc_eta, "max_inner": args.dc_max_inner,
+                              "fp32_stall": args.dc_fp32_stall, "outer_m": args.dc_outer_m,
+                              "precond": args.dc_precond,
+                              "metric_freeze": args.dc_metric_freeze,
+                              "cap_abort": args.dc_cap_abort,
+                              "cap_refresh": args.dc_cap_refresh},
+                   "warmstart": args.warmstart, "retry": bool(args.retry),
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "256 MB buffer written before each timed step"},
         "timed_steps": f"{args.steps} consecutive time steps from the initial markers; a "
@@ -761,11 +768,11 @@ def main(argv=None):
     ap.add_argument("--dc-fp32-window", type=int, default=0,
                     help="leave FP32 outer maps after this many maps without a new best "
                          "residual (0: after the first map below the stall cut)")
-    ap.add_argument("--dc-outer-m", type=int, default=5,
+    ap.add_argument("--dc-outer-m", type=int, default=0,
                     help="Anderson depth over the defect correction's outer iterates")
     ap.add_argument("--dc-cap-refresh", type=int, default=0, choices=[0, 1],
                     help="rebuild the FP32 metric after an inner solve that hit max_inner")
-    ap.add_argument("--dc-cap-abort", type=int, default=0,
+    ap.add_argument("--dc-cap-abort", type=int, default=2,
                     help="stagnation exit after this many FP64-stage outer maps in a row whose "
                          "inner solve hit max_inner without a new best (0: off)")
     ap.add_argument("--dc-precond", type=int, default=0, choices=[0, 1, 2],

@@ -542,12 +542,15 @@ def step_defect(ws: Workspace, v1, v0, w_parts, S0: float, dt: float, *, m: int 
                 stag_window: int = 5, stag_rel_tol: float = 0.1, use_gonzalez: bool = True,
                 precision: str = "fp64", metric64: bool = True, fp32_stall: float = 0.5,
                 outer_m: int = 0, precond: int = 0, metric_freeze: float = 0.0,
-                fp32_window: int = 0):
+                fp32_window: int = 0, cap_refresh: int = 0, cap_abort: int = 0):
     """step_defect! (solver.jl:569-634) on the device; v1 (guess) is overwritten with
     the solution. Returns (outer_iterations, residual, inner_iterations, initial_residual).
     outer_m > 0 mixes the outer iterates by Anderson and precond = 1 preconditions the
     inner iteration per marker (0, 0 = the reference's algorithm); metric_freeze > 0
-    stops rebuilding the FP32 metric once ||r|| < metric_freeze ||r_1||."""
+    stops rebuilding the FP32 metric once ||r|| < metric_freeze ||r_1||; cap_refresh
+    rebuilds it after an inner solve that hit max_inner; cap_abort = K leaves through
+    the stagnation exit once K FP64-stage outer maps in a row ended in a capped inner
+    solve without a new best outer residual."""
     v0 = _markers(v0, name="v0")
     N = v0.shape[0]
     v1 = _out(v1, (N, 2), "v1")
@@ -555,7 +558,8 @@ def step_defect(ws: Workspace, v1, v0, w_parts, S0: float, dt: float, *, m: int 
                   stag_rel_tol=stag_rel_tol, use_gonzalez=int(use_gonzalez),
                   precision=_PREC[precision])
     d = CoDefectOpts(eta, max_inner, stag_window, fp32_stall, int(metric64), int(outer_m),
-                     int(precond), float(metric_freeze), int(fp32_window))
+                     int(precond), float(metric_freeze), int(fp32_window), int(cap_refresh),
+                     int(cap_abort))
     it, inner = C.c_int(), C.c_int()
     res, r0 = C.c_double(), C.c_double()
     _check(ws.lib.co_step_defect(ws.h, C.byref(o), C.byref(d), _p(v1), _p(v0),

@@ -88,3 +88,38 @@ def test_stagnation_exit_returns_best_iterate(built_lib, oracle_mod, collops_mod
     assert abs(info[1] - info_ref[1]) <= 1e-9 * info_ref[1]
     assert np.max(np.abs(x - ref)) / np.max(np.abs(ref)) < 1e-11
     assert np.max(np.abs((w[:, None] * (x - v)).sum(0))) < 1e-12
+
+
+def test_cap_abort_leaves_early_with_best_iterate(built_lib, collops_mod):
+    """cap_abort (the library's extension of step_defect!): with max_inner = 1 and
+    an inner tolerance no single inner map can meet, every inner solve hits the
+    cap, so once two FP64-stage outer maps in a row bring no new best outer
+    residual the step leaves through the stagnation exit, far below max_iter,
+    with a state that conserves momentum (the best iterate's Picard update).
+    Without cap_abort the same step runs until the stagnation window exits or it
+    converges, and never with fewer outer maps. A negative cap_abort is refused."""
+    bp = uniform_bp(-6.0, 6.0, 16)
+    v, w = gaussian_markers(2048, 1.0, 0.5, seed=5)
+    ws = collops_mod.build_workspace(collops_mod.SimParameters(bp1=bp, bp2=bp))
+    f = np.zeros(ws.n_dofs)
+    collops_mod.l2_project_gpu(ws, f, v, w)
+    S0 = collops_mod.compute_entropy_gpu(ws, f)
+    dt = 0.05
+    v1 = np.zeros((2048, 2), order="F")
+    collops_mod.predictor(ws, v1, v, w, dt)
+    kw = dict(m=8, tol=1e-12, abs_floor=0.0, damping=0.7, max_iter=200, eta=1e-6, max_inner=1,
+              stag_window=10, stag_rel_tol=1e-3, metric64=True)
+    x_on = np.array(v1, order="F", copy=True)
+    info_on = collops_mod.step_defect(ws, x_on, v, w, S0, dt, cap_abort=2, **kw)
+    x_off = np.array(v1, order="F", copy=True)
+    info_off = collops_mod.step_defect(ws, x_off, v, w, S0, dt, cap_abort=0, **kw)
+    with pytest.raises(collops_mod.CollopsError) as ei:
+        collops_mod.step_defect(ws, np.array(v1, order="F", copy=True), v, w, S0, dt,
+                                cap_abort=-1, **kw)
+    ws.close()
+    print(f"cap_abort=2: {info_on}  cap_abort=0: {info_off}")
+    assert ei.value.status == 1
+    assert info_on[0] < 200 and info_on[0] <= info_off[0]
+    for x in (x_on, x_off):
+        assert np.all(np.isfinite(x))
+        assert np.max(np.abs((w[:, None] * (x - v)).sum(0))) < 1e-12
