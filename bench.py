@@ -72,7 +72,7 @@ WORKLOAD = dict(name="landau_n131072_mesh64_dt0.02", N=131072, n_el=64, lo=-6.0,
 # benchmark on GB300 (step 0 from the initial markers). The reference arm
 # scales its measured per-map time by it: a converged CPU step takes far longer
 # than the few minutes a benchmark run may take.
-FP64_MAPS_PER_STEP = 215
+FP64_MAPS_PER_STEP = 284
 FP64_MAPS_SOURCE = ("plain FP64 step 0 of this workload on GB300 (plain_fp64.iterations + 1 of "
                     "python bench.py)")
 C1 = dict(name="landau_n2048_mesh16_dt0.05", N=2048, n_el=16, lo=-6.0, hi=6.0, sx=1.0, sy=0.5,
