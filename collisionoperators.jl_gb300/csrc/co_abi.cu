@@ -180,7 +180,7 @@ static void free_ctx(co_ctx *c) {
                     c->mb.sphi, c->mb.px, c->mb.pg, c->mb.pw, c->mb.pf_x, c->mb.pf_g, c->mb.pf_w, c->mb.pf_wl,
                     c->mb.pdot, c->mb.pA, c->mb.part, c->mb.hist, c->mb.hoff, c->mb.count,
                     c->mb.cstart, c->mb.red, c->mb.dF, c->mb.dG, c->mb.Gk, c->mb.Phi,
-                    c->mb.Adef, c->mb.aa, c->mb.pc, c->st2, c->st3};
+                    c->mb.Adef, c->mb.aa, c->mb.pc, c->st2, c->st3, c->tickets};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     co_step_free(c);
@@ -196,7 +196,11 @@ extern "C" int co_ctx_create(const double *bp1, int nb1, const double *bp2, int 
                              int n_quad, unsigned flags, int device, co_ctx **out) {
     if (!out) return CO_ERR_ARG;
     *out = nullptr;
-    if (!bp1 || !bp2 || nb1 < 2 || nb2 < 2 || n_quad < 1 || n_quad > 8) return CO_ERR_ARG;
+    // nb1 - 1 <= 4096 cells per dimension: the fused dof-gather + mass kernel
+    // holds one column of nb1 + 1 dofs in shared memory
+    if (!bp1 || !bp2 || nb1 < 2 || nb2 < 2 || nb1 > 4097 || nb2 > 4097 || n_quad < 1 ||
+        n_quad > 8)
+        return CO_ERR_ARG;
     if (p_deg != 2) return CO_ERR_UNSUPPORTED;
     for (int i = 0; i + 1 < nb1; i++)
         if (!(bp1[i + 1] > bp1[i])) return CO_ERR_ARG;
@@ -309,6 +313,11 @@ extern "C" int co_ctx_create(const double *bp1, int nb1, const double *bp2, int 
     if (cudaMalloc(&c->mb.red, sizeof(double) * CO_RED_CAP * CO_RED_COMPS + 64) != cudaSuccess)
         { free_ctx(c); return CO_ERR_NOMEM; };
     if (cudaMalloc(&c->st, sizeof(co_solver_state)) != cudaSuccess) { free_ctx(c); return CO_ERR_NOMEM; };
+    if (cudaMalloc(&c->tickets, sizeof(unsigned) * CO_TICKETS) != cudaSuccess ||
+        cudaMemset(c->tickets, 0, sizeof(unsigned) * CO_TICKETS) != cudaSuccess) {
+        free_ctx(c);
+        return CO_ERR_NOMEM;
+    }
     if (cudaMallocHost(&c->st_host, sizeof(co_solver_state)) != cudaSuccess) { free_ctx(c); return CO_ERR_NOMEM; };
     memset(c->st_host, 0, sizeof(co_solver_state));
     if (cudaMemset(c->st, 0, sizeof(co_solver_state)) != cudaSuccess) { free_ctx(c); return CO_ERR_CUDA; };

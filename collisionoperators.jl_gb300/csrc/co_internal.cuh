@@ -19,6 +19,10 @@
 
 #define CO_CHUNK 1024        // markers per sort chunk (one block of 1024 threads)
 #define CO_RED_THREADS 256   // threads of the reduction-producing kernels
+#define CO_TICKETS 8         // arrival counters per context (ctx.tickets)
+#define CO_TICKET_FROZEN 2   // k_frozen_map's counter (0, 1: k_cellcount per set)
+#define CO_TICKET_LAMBDA 3   // k_grad_L's counter when it forms lambda
+#define CO_TICKET_WINDOW 4   // k_anderson_cols's counter when it solves the window
 #define CO_MAX_M 8           // Anderson depth limit of the device solver
 #define CO_FS_FLOOR 1e-30    // functions.jl:23
 #define CO_G_MAX 100.0       // functions.jl:31
@@ -95,6 +99,16 @@ struct co_sortset {
     double *xi, *sw, *sphi, *bS, *b, *y;
 };
 
+// The Gonzalez lambda formed by the last block of k_grad_L (st == nullptr: not)
+struct co_lambda_job {
+    co_solver_state *st;
+    double S0;
+    int gonzalez;
+    const double *Ep;   // element entropy partials of v_in (S1 = their sum), or nullptr: st->S1
+    int n_el;
+    unsigned *ticket;
+};
+
 struct co_ctx {
     int device;
     cudaStream_t stream;
@@ -117,6 +131,10 @@ struct co_ctx {
     double *Ep;              // element entropy partials [n_el]
     co_sortset gs;           // sort/projection set 1 (Gonzalez v_in), allocated on use
     int gs_cap;              // marker capacity of gs (0: not allocated)
+    // arrival counters of the kernels whose last block finishes the launch's work
+    // (k_cellcount: one per marker set; k_frozen_map: slot CO_TICKET_FROZEN); each
+    // last block resets its counter, so launches and graph replays reuse them
+    unsigned *tickets;
     co_bufs mb;
     co_solver_state *st;     // device state
     co_solver_state *st2;    // inner-solve state of the defect correction
@@ -164,6 +182,14 @@ int co_project_two(co_ctx *c, double *f0, double *f1, int two);
 // r-local of f (-> dof vector r) and, with fS != nullptr, the entropy partials of
 // fS (-> Ep), in one quadrature launch
 int co_r_and_entropy_dev(co_ctx *c, const double *f, double *r, const double *fS);
+// L = M^{-1} r(f) (quadrature, dof gather and mass solve in three launches) and,
+// with fS != nullptr, the entropy partials of fS (-> Ep) in the quadrature launch
+int co_r_solve_dev(co_ctx *c, const double *f, double *L, const double *fS);
+// co_grad_L_dev with dS and the Gonzalez partials, and lambda into ctx->st (the
+// last block of the launch): S1 from Ep (element entropy partials) or st->S1
+int co_grad_L_lambda_dev(co_ctx *c, const double *x, int N, const double *L, double *G,
+                         const double *w, double *dS, const double *dv, double *red,
+                         double S0, int gonzalez, const double *Ep);
 void co_sortset_free(co_ctx *c);
 int co_project_sorted(co_ctx *c, double *f_out);               // scatter + dof gather + mass solve
 int co_mass_solve_dev(co_ctx *c, const double *rhs, double *out);

@@ -40,6 +40,22 @@ __device__ __forceinline__ double co_strided_sum(const double *v, int i0, int n,
     return s;
 }
 
+// co_strided_sum with the loads through L2 (__ldcg), for partials that other
+// blocks of the same launch wrote (the last-block-done pattern)
+__device__ __forceinline__ double co_strided_sum_cg(const double *v, int i0, int n, int step,
+                                                    int ncomp, int comp, double s) {
+    int i = i0;
+    for (; i + 7 * step < n; i += 8 * step) {
+        double t[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) t[u] = __ldcg(&v[(size_t)(i + u * step) * ncomp + comp]);
+#pragma unroll
+        for (int u = 0; u < 8; u++) s += t[u];
+    }
+    for (; i < n; i += step) s += __ldcg(&v[(size_t)i * ncomp + comp]);
+    return s;
+}
+
 // Sum of red[0..n) * (stride) component `comp` by one block, fixed order:
 // thread t sums entries t, t+B, ... in order, then co_block_sum.
 __device__ __forceinline__ double co_sum_partials(const double *red, int n, int ncomp,

@@ -54,13 +54,18 @@ static const char *prec_name(int p) {
 
 __global__ void __launch_bounds__(256)
 k_lambda(const double *__restrict__ red, int nred, co_solver_state *st, double S0,
-         int gonzalez) {
+         int gonzalez, const double *__restrict__ Ep, int n_el) {
     __shared__ double sh[32];
+    // with Ep: S1 = S(v_in) from the element entropy partials first (the sum
+    // k_sum_to forms, in the same order)
+    double S1 = Ep ? co_sum_partials(Ep, n_el, 1, 0, sh) : 0.0;
     double dot = co_sum_partials(red, nred, 2, 0, sh);
     double n2 = co_sum_partials(red, nred, 2, 1, sh);
     if (threadIdx.x == 0) {
+        if (Ep) st->S1 = S1;
+        else S1 = st->S1;
         double lam = 0.0;
-        if (gonzalez) lam = n2 > 1e-30 ? (st->S1 - S0 - dot) / n2 : 0.0;
+        if (gonzalez) lam = n2 > 1e-30 ? (S1 - S0 - dot) / n2 : 0.0;
         st->lambda = lam;
     }
 }
@@ -375,33 +380,35 @@ k_ctrl1(const double *__restrict__ red, int nred, co_solver_state *st, co_dev_op
     }
 }
 
-// damped Picard branch (solver.jl:384) + best-iterate tracking (:343-346)
-__global__ void k_plain_update(int n2, co_solver_state *st, int exit_picard,
-                               double *__restrict__ v1, const double *__restrict__ Gv,
-                               const double *__restrict__ r, double *__restrict__ rp,
-                               double *__restrict__ Gp, double *__restrict__ vbest) {
+__device__ void anderson_solve_body(const double *__restrict__ red, int nred,
+                                    co_solver_state *st, const co_dev_opts &o);
+
+// The iterate update after the control of iteration k, one launch for both
+// branches: the damped Picard branch (path 0, solver.jl:384; the former
+// k_plain_update) or the new window column (solver.jl:393-394) with its dot
+// products with the window and with r (path 1; block partials laid out
+// [block][2*CO_MAX_M], solved by the launch's last block); in both, the best-iterate copy
+// (solver.jl:343-346) when the residual improved.
+__global__ void __launch_bounds__(CO_RED_THREADS)
+k_anderson_cols(int n2, co_solver_state *st, int exit_picard, double *__restrict__ v1,
+                const double *__restrict__ r, double *__restrict__ rp,
+                const double *__restrict__ Gv, double *__restrict__ Gp,
+                double *__restrict__ dF, double *__restrict__ dG, size_t ldF,
+                double *__restrict__ vbest, double *__restrict__ red, co_dev_opts o,
+                unsigned *ticket) {
     if (st->done) return;
-    int path = st->path, improved = st->improved;
-    double damp = st->damp;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
-        double x = v1[i], g = Gv[i];
-        if (improved) vbest[i] = exit_picard ? g : x;
-        if (path == 0) {
+    const int improved = st->improved;
+    if (st->path != 1) {
+        const double damp = st->damp;
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
+            double x = v1[i], g = Gv[i];
+            if (improved) vbest[i] = exit_picard ? g : x;
             v1[i] = damp * g + (1 - damp) * x;
             rp[i] = r[i];
             Gp[i] = g;
         }
+        return;
     }
-}
-
-// new window column (solver.jl:393-394) and its dot products with the window
-// and with r; block partials laid out [block][2*CO_MAX_M]
-__global__ void __launch_bounds__(CO_RED_THREADS)
-k_anderson_cols(int n2, co_solver_state *st, const double *__restrict__ r,
-                double *__restrict__ rp, const double *__restrict__ Gv, double *__restrict__ Gp,
-                double *__restrict__ dF, double *__restrict__ dG, size_t ldF,
-                double *__restrict__ red) {
-    if (st->done || st->path != 1) return;
     const int slot = st->slot - 1, hist = st->history;
     // the window loops run to CO_MAX_M, unrolled with a guard, so that pa, pb
     // stay in registers (a runtime bound would put them in local memory)
@@ -410,6 +417,7 @@ k_anderson_cols(int n2, co_solver_state *st, const double *__restrict__ r,
     for (int j = 0; j < CO_MAX_M; j++) pa[j] = pb[j] = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
         double ri = r[i], gi = Gv[i];
+        if (improved) vbest[i] = exit_picard ? gi : v1[i];
         double F = ri - rp[i];
         double Gd = gi - Gp[i];
         dF[(size_t)slot * ldF + i] = F;
@@ -447,13 +455,24 @@ k_anderson_cols(int n2, co_solver_state *st, const double *__restrict__ r,
         for (int w = 0; w < nw; w++) s += wsum[w][t];
         red[(size_t)blockIdx.x * 2 * CO_MAX_M + t] = s;
     }
+    // the last block to finish solves for the mixing coefficients
+    __shared__ int last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (threadIdx.x == 0) *ticket = 0u;
+    anderson_solve_body(red, gridDim.x, st, o);
 }
 
-// normal equations with Tikhonov shift, gamma = ATA \ ATr (solver.jl:396-409)
-__global__ void __launch_bounds__(256)
-k_anderson_solve(const double *__restrict__ red, int nred, co_solver_state *st, co_dev_opts o) {
+// normal equations with Tikhonov shift, gamma = ATA \ ATr (solver.jl:396-409),
+// from the nred block partials of the new Gram row and of A^T r; run by the last
+// block (256 threads) of k_anderson_cols, which wrote the partials
+__device__ void anderson_solve_body(const double *__restrict__ red, int nred,
+                                    co_solver_state *st, const co_dev_opts &o) {
     __shared__ double dots[2 * CO_MAX_M];
-    if (st->done || st->path != 1) return;
     const int slot = st->slot - 1, h = st->history;
     // the 2h sums over the nred block partials: one warp per value, lanes stride
     // the partials in order, then a shuffle tree (fixed order)
@@ -461,104 +480,103 @@ k_anderson_solve(const double *__restrict__ red, int nred, co_solver_state *st, 
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
         for (int c = warp; c < 2 * h; c += nw) {
             const int col = c < h ? c : CO_MAX_M + (c - h);
-            double s = co_strided_sum(red, lane, nred, 32, 2 * CO_MAX_M, col, 0.0);
+            double s = co_strided_sum_cg(red, lane, nred, 32, 2 * CO_MAX_M, col, 0.0);
             for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
             if (lane == 0) dots[col] = s;
         }
     }
-    // the cached Gram matrix through shared memory: the one thread that solves
-    // then reads it at shared-memory latency
+    // the cached Gram matrix through shared memory, with the new row and column
     __shared__ double sA[CO_MAX_M * CO_MAX_M];
     for (int t = threadIdx.x; t < CO_MAX_M * CO_MAX_M; t += blockDim.x) sA[t] = st->ATA[t];
     __syncthreads();
-    if (threadIdx.x != 0) return;
-    for (int j = 0; j < h; j++) {
-        sA[slot * CO_MAX_M + j] = dots[j];
-        sA[j * CO_MAX_M + slot] = dots[j];
-        st->ATA[slot * CO_MAX_M + j] = dots[j];
-        st->ATA[j * CO_MAX_M + slot] = dots[j];
-    }
-    // LU with partial pivoting on the leading h x h block. Every loop runs to
-    // CO_MAX_M, unrolled with guards, and row swaps are predicated moves, so A
-    // and b live in registers; the operations on the h x h block and their
-    // order are those of the plain loops.
-    double A[CO_MAX_M][CO_MAX_M], b[CO_MAX_M];
+    if (threadIdx.x >= 32) return;
+    const int lane = threadIdx.x;
+    if (lane == 0)
+        for (int j = 0; j < h; j++) {
+            sA[slot * CO_MAX_M + j] = dots[j];
+            sA[j * CO_MAX_M + slot] = dots[j];
+            st->ATA[slot * CO_MAX_M + j] = dots[j];
+            st->ATA[j * CO_MAX_M + slot] = dots[j];
+        }
+    __syncwarp();
+    // LU with partial pivoting on the leading h x h block, by one warp: lane r
+    // holds row r of A and b[r]. Each element sees the operations of the
+    // sequential algorithm in the same order (pivot: the first row of largest
+    // |A[i][k]|; L stored below the diagonal; b permuted as the rows; forward
+    // substitution in ascending j, back substitution in ascending j per row),
+    // but the rows of one elimination step and the forward updates run on
+    // different lanes, so the chain is ~h steps long instead of ~h^3 / 3.
+    double a[CO_MAX_M];
 #pragma unroll
-    for (int i = 0; i < CO_MAX_M; i++) {
+    for (int j = 0; j < CO_MAX_M; j++)
+        a[j] = (lane < h && j < h) ? sA[lane * CO_MAX_M + j] : 0.0;
+    double bb = lane < h ? dots[CO_MAX_M + lane] : 0.0;
+    double dm = 0.0;
+    for (int j = 0; j < h; j++) dm += sA[j * CO_MAX_M + j];
+    dm /= h;
+    const double l2 = o.reg_factor * dm + 1e-30;
+#pragma unroll
+    for (int j = 0; j < CO_MAX_M; j++)
+        if (j == lane && lane < h) a[j] += l2;
+    for (int k = 0; k < h; k++) {
+        double akk = 0.0;   // this lane's A[lane][k]
 #pragma unroll
         for (int j = 0; j < CO_MAX_M; j++)
-            A[i][j] = (i < h && j < h) ? sA[i * CO_MAX_M + j] : 0.0;
-        b[i] = i < h ? dots[CO_MAX_M + i] : 0.0;
-    }
-    double dm = 0.0;
+            if (j == k) akk = a[j];
+        const bool cand = lane >= k && lane < h;
+        double mx = cand ? fabs(akk) : -1.0;
 #pragma unroll
-    for (int j = 0; j < CO_MAX_M; j++)
-        if (j < h) dm += A[j][j];
-    dm /= h;
-    double l2 = o.reg_factor * dm + 1e-30;
+        for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+        const unsigned ball = __ballot_sync(0xffffffffu, cand && fabs(akk) == mx);
+        const int p = ball ? __ffs(ball) - 1 : k;
+        if (p != k) {   // swap rows k and p (and b)
+            const int src = lane == k ? p : (lane == p ? k : lane);
 #pragma unroll
-    for (int j = 0; j < CO_MAX_M; j++)
-        if (j < h) A[j][j] += l2;
-    int piv[CO_MAX_M];
+            for (int j = 0; j < CO_MAX_M; j++) a[j] = __shfl_sync(0xffffffffu, a[j], src);
+            bb = __shfl_sync(0xffffffffu, bb, src);
+        }
+        double rk[CO_MAX_M];   // pivot row
 #pragma unroll
-    for (int k = 0; k < CO_MAX_M; k++) {
-        if (k >= h) continue;
-        int p = k;
-        double mx = fabs(A[k][k]);
+        for (int j = 0; j < CO_MAX_M; j++) rk[j] = __shfl_sync(0xffffffffu, a[j], k);
+        if (lane > k && lane < h) {
+            double f = 0.0;
 #pragma unroll
-        for (int i = k + 1; i < CO_MAX_M; i++)
-            if (i < h && fabs(A[i][k]) > mx) {
-                mx = fabs(A[i][k]);
-                p = i;
-            }
-        piv[k] = p;
-#pragma unroll
-        for (int i = k + 1; i < CO_MAX_M; i++)
-            if (i == p)
-#pragma unroll
-                for (int j = 0; j < CO_MAX_M; j++) {
-                    double t = A[k][j];
-                    A[k][j] = A[i][j];
-                    A[i][j] = t;
+            for (int j = 0; j < CO_MAX_M; j++)
+                if (j == k) {
+                    a[j] /= rk[j];
+                    f = a[j];
                 }
 #pragma unroll
-        for (int i = k + 1; i < CO_MAX_M; i++) {
-            if (i < h) {
-                A[i][k] /= A[k][k];
-#pragma unroll
-                for (int j = k + 1; j < CO_MAX_M; j++)
-                    if (j < h) A[i][j] -= A[i][k] * A[k][j];
-            }
+            for (int j = 0; j < CO_MAX_M; j++)
+                if (j > k && j < h) a[j] -= f * rk[j];
         }
     }
+    // forward substitution with the unit lower factor
+    for (int j = 0; j + 1 < h; j++) {
+        const double bj = __shfl_sync(0xffffffffu, bb, j);
+        double aij = 0.0;
 #pragma unroll
-    for (int k = 0; k < CO_MAX_M; k++) {
-        if (k >= h) continue;
-#pragma unroll
-        for (int i = k + 1; i < CO_MAX_M; i++)
-            if (piv[k] == i) {
-                double t = b[k];
-                b[k] = b[i];
-                b[i] = t;
-            }
+        for (int t = 0; t < CO_MAX_M; t++)
+            if (t == j) aij = a[t];
+        if (lane > j && lane < h) bb -= aij * bj;
     }
+    // back substitution, row by row from the last
+    for (int i = h - 1; i >= 0; i--) {
+        for (int j = i + 1; j < h; j++) {
+            const double bj = __shfl_sync(0xffffffffu, bb, j);
+            double aij = 0.0;
 #pragma unroll
-    for (int i = 0; i < CO_MAX_M; i++)
-#pragma unroll
-        for (int j = 0; j < i; j++)
-            if (i < h) b[i] -= A[i][j] * b[j];
-#pragma unroll
-    for (int i = CO_MAX_M - 1; i >= 0; i--) {
-        if (i < h) {
-#pragma unroll
-            for (int j = i + 1; j < CO_MAX_M; j++)
-                if (j < h) b[i] -= A[i][j] * b[j];
-            b[i] /= A[i][i];
+            for (int t = 0; t < CO_MAX_M; t++)
+                if (t == j) aij = a[t];
+            if (lane == i) bb -= aij * bj;
         }
-    }
+        double aii = 1.0;
 #pragma unroll
-    for (int j = 0; j < CO_MAX_M; j++)
-        if (j < h) st->gamma[j] = b[j];
+        for (int t = 0; t < CO_MAX_M; t++)
+            if (t == i) aii = a[t];
+        if (lane == i) bb /= aii;
+    }
+    if (lane < h) st->gamma[lane] = bb;
 }
 
 // v1 = damp (Gv - dG gamma) + (1 - damp) v_old (solver.jl:410-412)
@@ -658,12 +676,15 @@ int co_lb_fused(co_ctx *c, int N, double nu, double dt, double *Gv, const double
 static int landau_tail(co_ctx *c, int gonzalez, int N, double S0, int nred) {
     int rc;
     co_bufs &b = c->mb;
-    if ((rc = co_r_and_entropy_dev(c, c->f, c->rr, gonzalez ? c->fin : nullptr))) return rc;
-    if (gonzalez && (rc = co_entropy_finalize_dev(c, &c->st->S1))) return rc;
-    if ((rc = co_mass_solve_dev(c, c->rr, c->L))) return rc;
-    if ((rc = co_grad_L_dev(c, b.vmid, N, c->L, b.G, b.w, b.dS, b.dv, b.red))) return rc;
-    k_lambda<<<1, 256, 0, c->stream>>>(b.red, nred, c->st, S0, gonzalez);
+    if ((rc = co_r_solve_dev(c, c->f, c->L, gonzalez ? c->fin : nullptr))) return rc;
+    // grad L with dS and the Gonzalez partials; its last block forms lambda
+    if (N > 0)
+        return co_grad_L_lambda_dev(c, b.vmid, N, c->L, b.G, b.w, b.dS, b.dv, b.red, S0,
+                                    gonzalez, gonzalez ? c->Ep : nullptr);
+    k_lambda<<<1, 256, 0, c->stream>>>(b.red, 0, c->st, S0, gonzalez,
+                                       gonzalez ? c->Ep : nullptr, c->n_el);
     c->launches++;
+    (void)nred;
     CO_CK(cudaGetLastError());
     return CO_OK;
 }
@@ -694,12 +715,10 @@ static int picard_map_impl(co_ctx *c, int model, int gonzalez, double nu, int pr
     int nred = red_blocks(c, N);
     if ((rc = project_mid(c, gonzalez, vin, v0, N))) return rc;
     if (model == CO_MODEL_LB) {
-        if (gonzalez) {
-            if ((rc = co_entropy_parts_dev(c, c->fin))) return rc;
-            if ((rc = co_entropy_finalize_dev(c, &c->st->S1))) return rc;
-        }
+        if (gonzalez && (rc = co_entropy_parts_dev(c, c->fin))) return rc;
         if ((rc = co_loggrad_dev(c, b.vmid, N, c->f, b.G, b.w, b.dv, b.red))) return rc;
-        k_lambda<<<1, 256, 0, c->stream>>>(b.red, nred, c->st, S0, gonzalez);
+        k_lambda<<<1, 256, 0, c->stream>>>(b.red, nred, c->st, S0, gonzalez,
+                                           gonzalez ? c->Ep : nullptr, c->n_el);
         c->launches++;
         CO_CK(cudaGetLastError());
         if (c->lb_two_pass) {
@@ -788,16 +807,15 @@ static int anderson_loop(co_ctx *c, const co_opts *o, int precision, int N, doub
                                   b.v0, N, S0, dt, b.r, &nred)))
             return rc;
         k_ctrl1<<<1, 256, 0, c->stream>>>(b.red, nred, c->st, d);
-        k_plain_update<<<eg, 256, 0, c->stream>>>(n2, c->st, o->exit_picard_step, b.v1, b.Gv, b.r,
-                                                  b.rp, b.Gp, b.vbest);
+        const int ng = window_blocks(c, n2);
+        k_anderson_cols<<<ng, CO_RED_THREADS, 0, c->stream>>>(n2, c->st, o->exit_picard_step, b.v1,
+                                                              b.r, b.rp, b.Gv, b.Gp, b.dF, b.dG,
+                                                              ldF, b.vbest, b.red, d,
+                                                              c->tickets + CO_TICKET_WINDOW);
         c->launches += 2;
         if (o->use_anderson) {
-            int ng = window_blocks(c, n2);
-            k_anderson_cols<<<ng, CO_RED_THREADS, 0, c->stream>>>(n2, c->st, b.r, b.rp, b.Gv, b.Gp,
-                                                                  b.dF, b.dG, ldF, b.red);
-            k_anderson_solve<<<1, 256, 0, c->stream>>>(b.red, ng, c->st, d);
             k_anderson_update<<<eg, 256, 0, c->stream>>>(n2, c->st, b.v1, b.Gv, b.dG, ldF);
-            c->launches += 3;
+            c->launches += 1;
         }
         CO_CK(cudaGetLastError());
         CO_CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(co_solver_state), cudaMemcpyDeviceToHost,
@@ -923,12 +941,19 @@ __global__ void k_geff_store(int N, const double *__restrict__ dS, const double 
 }
 
 // frozen_map! (solver.jl:585-595): Phi = Gv - dt A (G_eff(u) - Gk), r = Phi - u
+__device__ void ctrl_inner_body(const double *__restrict__ red, int nred, co_solver_state *si,
+                                const co_solver_state *so, int m, double damping,
+                                cudaGraphConditionalHandle hnd, int use_cond, int cap,
+                                double *sh);
+
 __global__ void __launch_bounds__(CO_RED_THREADS)
 k_frozen_map(int N, const double *__restrict__ Gv, const double *__restrict__ A,
              const double *__restrict__ Gk, const double *__restrict__ dS,
              const double *__restrict__ dv, const double *__restrict__ w,
              const co_solver_state *st, int use_lambda, double dt, const double *__restrict__ u,
-             double *__restrict__ Phi, double *__restrict__ r, double *__restrict__ red) {
+             double *__restrict__ Phi, double *__restrict__ r, double *__restrict__ red,
+             co_solver_state *si, int m, double damping, cudaGraphConditionalHandle hnd,
+             int use_cond, int cap, unsigned *ticket) {
     __shared__ double sh[32];
     double lam = use_lambda ? st->lambda : 0.0;
     double sr = 0.0;
@@ -951,6 +976,16 @@ k_frozen_map(int N, const double *__restrict__ Gv, const double *__restrict__ A,
         red[blockIdx.x * 2 + 0] = s;
         red[blockIdx.x * 2 + 1] = 0.0;
     }
+    // the last block to finish runs the inner control on all blocks' partials
+    __shared__ int last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (threadIdx.x == 0) *ticket = 0u;
+    ctrl_inner_body(red, gridDim.x, si, st, m, damping, hnd, use_cond, cap, sh);
 }
 
 // Block-Newton preconditioner of the inner iteration (co_defect_opts.precond):
@@ -1079,12 +1114,19 @@ __global__ void k_defect_best(int n2, const co_solver_state *st, const double *_
 }
 
 // inner Anderson control (solver.jl:497-521): tolerance from the outer state
-__global__ void __launch_bounds__(256)
-k_ctrl_inner(const double *__restrict__ red, int nred, co_solver_state *si,
-             const co_solver_state *so, int m, double damping) {
-    __shared__ double sh[32];
-    if (si->done) return;
-    double r2 = co_sum_partials(red, nred, 2, 0, sh);
+// Inner-iteration control (after the frozen map's residual): the residual
+// norm, the exit test against the outer stage's tolerance, and the Anderson
+// window bookkeeping; inside the device-side inner loop also the loop
+// condition. Run by the last block of k_frozen_map, whose partials it sums.
+__device__ void ctrl_inner_body(const double *__restrict__ red, int nred, co_solver_state *si,
+                                const co_solver_state *so, int m, double damping,
+                                cudaGraphConditionalHandle hnd, int use_cond, int cap,
+                                double *sh) {
+    if (si->done) {
+        if (use_cond && threadIdx.x == 0) cudaGraphSetConditional(hnd, 0u);
+        return;
+    }
+    double r2 = co_block_sum(co_strided_sum_cg(red, threadIdx.x, nred, blockDim.x, 2, 0, 0.0), sh);
     if (threadIdx.x != 0) return;
     int k = si->k + 1;
     si->k = k;
@@ -1094,20 +1136,22 @@ k_ctrl_inner(const double *__restrict__ red, int nred, co_solver_state *si,
     if (!isfinite(nrm)) {
         si->error = CO_ERR_NONFINITE;
         si->done = 4;
-        return;
-    }
-    if (nrm < so->res_out) {
+    } else if (nrm < so->res_out) {
         si->done = 1;
-        return;
-    }
-    si->damp = damping;
-    if (k == 1) {
-        si->path = 0;
     } else {
-        si->path = 1;
-        si->slot = si->slot % m + 1;
-        si->history = si->history + 1 < m ? si->history + 1 : m;
+        si->damp = damping;
+        if (k == 1) {
+            si->path = 0;
+        } else {
+            si->path = 1;
+            si->slot = si->slot % m + 1;
+            si->history = si->history + 1 < m ? si->history + 1 : m;
+        }
     }
+    // inside the device-side inner loop: repeat the body while the inner solve
+    // has not exited and fewer than cap iterations ran
+    if (use_cond)
+        cudaGraphSetConditional(hnd, (!si->done && !si->error && k < cap) ? 1u : 0u);
 }
 
 // Anderson mixing of the outer iterates (co_defect_opts.outer_m > 0): the
@@ -1157,14 +1201,6 @@ __global__ void k_copy_if_done(int n2, const co_solver_state *st, int want, doub
     if (st->done != want) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x)
         dst[i] = src[i];
-}
-
-// Condition of the device-side inner loop: repeat while the inner solve has not
-// exited (converged, error) and fewer than cap iterations ran.
-__global__ void k_inner_continue(cudaGraphConditionalHandle h, const co_solver_state *si,
-                                 int cap) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    cudaGraphSetConditional(h, (!si->done && !si->error && si->k < cap) ? 1u : 0u);
 }
 
 static bool co_inner_host_loop() {
@@ -1242,12 +1278,15 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
     }
     // one inner iteration: G_eff at u, the frozen-metric map Phi(u) and its
     // residual, the Anderson control and update of u (= v1, in place)
-    auto inner_iteration = [&]() -> int {
+    auto inner_iteration = [&](cudaGraphConditionalHandle hnd, int use_cond) -> int {
         int rc;
         if ((rc = landau_geff_dev(c, gz, b.v1, b.v0, N, S0))) return rc;
-        k_frozen_map<<<nred, CO_RED_THREADS, 0, c->stream>>>(N, b.Gv, b.Adef, b.Gk, b.dS, b.dv,
-                                                           b.w, c->st, gz, dt, b.v1, b.Phi, b.r,
-                                                           b.red);
+        // the frozen map, and in its last block the inner control (residual
+        // norm, exit test, window bookkeeping, loop condition)
+        k_frozen_map<<<nred, CO_RED_THREADS, 0, c->stream>>>(
+            N, b.Gv, b.Adef, b.Gk, b.dS, b.dv, b.w, c->st, gz, dt, b.v1, b.Phi, b.r, b.red,
+            c->st2, o->m, o->damping, hnd, use_cond, dopt->max_inner,
+            c->tickets + CO_TICKET_FROZEN);
         // the map Anderson iterates and its residual: Phi, r -- or, with the
         // preconditioner, Psi = u + P^{-1} r and P^{-1} r
         double *mapv = b.Phi, *res = b.r;
@@ -1260,21 +1299,20 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
             mapv = pc_Psi;
             res = pc_z;
         }
-        k_ctrl_inner<<<1, 256, 0, c->stream>>>(b.red, nred, c->st2, c->st, o->m, o->damping);
-        k_plain_update<<<eg, 256, 0, c->stream>>>(n2, c->st2, 0, b.v1, mapv, res, b.rp, b.Gp,
-                                                  b.vbest);
         int ng = window_blocks(c, n2);
-        k_anderson_cols<<<ng, CO_RED_THREADS, 0, c->stream>>>(n2, c->st2, res, b.rp, mapv,
-                                                              b.Gp, b.dF, b.dG, ldF, b.red);
-        k_anderson_solve<<<1, 256, 0, c->stream>>>(b.red, ng, c->st2, di);
+        k_anderson_cols<<<ng, CO_RED_THREADS, 0, c->stream>>>(n2, c->st2, 0, b.v1, res, b.rp,
+                                                              mapv, b.Gp, b.dF, b.dG, ldF,
+                                                              b.vbest, b.red, di,
+                                                              c->tickets + CO_TICKET_WINDOW);
         k_anderson_update<<<eg, 256, 0, c->stream>>>(n2, c->st2, b.v1, mapv, b.dG, ldF);
-        c->launches += 6;
+        c->launches += 3;
         CO_CK(cudaGetLastError());
         return CO_OK;
     };
     // The inner loop runs on the device: inner_iteration is captured once per
-    // call as the body of a conditional WHILE node, and k_inner_continue ends it
-    // when the inner solve exits or max_inner iterations ran. The host launches
+    // call as the body of a conditional WHILE node, and the inner control (the
+    // last block of k_frozen_map) ends it when the inner solve exits or
+    // max_inner iterations ran. The host launches
     // one graph and waits once per outer iteration instead of once per inner
     // iteration (COLLOPS_INNER_LOOP=host restores the host-driven loop; both
     // run the same kernels on the same data and give identical results).
@@ -1303,12 +1341,7 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
         CO_CK(cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0,
                                             cudaStreamCaptureModeThreadLocal));
         const unsigned long long l0 = c->launches;
-        int r = inner_iteration();
-        if (!r) {
-            k_inner_continue<<<1, 32, 0, c->stream>>>(hnd, c->st2, dopt->max_inner);
-            c->launches++;
-            if (cudaGetLastError() != cudaSuccess) r = CO_ERR_CUDA;
-        }
+        int r = inner_iteration(hnd, 1);
         ig.body_launches = c->launches - l0;
         cudaError_t ce = cudaStreamEndCapture(c->stream, &body);
         if (r) return r;
@@ -1376,7 +1409,7 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
         int j;   // inner iterations run (max_inner + 1: the cap was reached)
         if (host_loop) {
             for (j = 1; j <= dopt->max_inner; j++) {
-                if ((rc = inner_iteration())) return rc;
+                if ((rc = inner_iteration(0, 0))) return rc;
                 CO_CK(cudaMemcpyAsync(c->st_host, c->st2, sizeof(co_solver_state),
                                       cudaMemcpyDeviceToHost, c->stream));
                 CO_CK(cudaStreamSynchronize(c->stream));
@@ -1392,7 +1425,7 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
                                   cudaMemcpyDeviceToHost, c->stream));
             CO_CK(cudaStreamSynchronize(c->stream));
             if (c->st_host->error) return c->st_host->error;
-            const int ran = c->st_host->k;   // k_ctrl_inner counts every iteration
+            const int ran = c->st_host->k;   // the inner control counts every iteration
             c->launches += (unsigned long long)(ran > 1 ? ran - 1 : 0) * ig.body_launches;
             j = c->st_host->done ? ran : dopt->max_inner + 1;
         }
@@ -1416,14 +1449,13 @@ int co_step_defect_buffers(co_ctx *c, const co_opts *o, const co_defect_opts *do
             k_ctrl_aa<<<1, 32, 0, c->stream>>>(c->st3, c->st, mo, stage != aa_stage);
             aa_stage = stage;
             k_aa_resid<<<eg, 256, 0, c->stream>>>(n2, c->st, b.v1, aa_vk, aa_u, aa_r);
-            k_plain_update<<<eg, 256, 0, c->stream>>>(n2, c->st3, 0, aa_vk, aa_u, aa_r, aa_rp,
-                                                      aa_Gp, b.vbest);
             int ng = window_blocks(c, n2);
-            k_anderson_cols<<<ng, CO_RED_THREADS, 0, c->stream>>>(n2, c->st3, aa_r, aa_rp, aa_u,
-                                                                  aa_Gp, aa_dF, aa_dG, ld2, b.red);
-            k_anderson_solve<<<1, 256, 0, c->stream>>>(b.red, ng, c->st3, di);
+            k_anderson_cols<<<ng, CO_RED_THREADS, 0, c->stream>>>(n2, c->st3, 0, aa_vk, aa_r,
+                                                                  aa_rp, aa_u, aa_Gp, aa_dF,
+                                                                  aa_dG, ld2, b.vbest, b.red, di,
+                                                                  c->tickets + CO_TICKET_WINDOW);
             k_anderson_update<<<eg, 256, 0, c->stream>>>(n2, c->st3, aa_vk, aa_u, aa_dG, ld2);
-            c->launches += 6;
+            c->launches += 4;
             CO_CK(cudaMemcpyAsync(b.v1, aa_vk, n2 * sizeof(double), cudaMemcpyDeviceToDevice,
                                   c->stream));
         }
@@ -1726,16 +1758,14 @@ static int batch_iteration_impl(co_batch *B, const co_opts *o, const double *S0,
         size_t ldF = 2 * (size_t)b.cap;
         cudaStream_t cs = c->stream;
         k_ctrl1<<<1, 256, 0, cs>>>(b.red, nred[i], c->st, d);
-        k_plain_update<<<eg, 256, 0, cs>>>(n2, c->st, o->exit_picard_step, b.v1, b.Gv, b.r, b.rp,
-                                           b.Gp, b.vbest);
         int ng = window_blocks(c, n2);
-        k_anderson_cols<<<ng, CO_RED_THREADS, 0, cs>>>(n2, c->st, b.r, b.rp, b.Gv, b.Gp, b.dF,
-                                                       b.dG, ldF, b.red);
-        k_anderson_solve<<<1, 256, 0, cs>>>(b.red, ng, c->st, d);
+        k_anderson_cols<<<ng, CO_RED_THREADS, 0, cs>>>(n2, c->st, o->exit_picard_step, b.v1, b.r,
+                                                       b.rp, b.Gv, b.Gp, b.dF, b.dG, ldF, b.vbest,
+                                                       b.red, d, c->tickets + CO_TICKET_WINDOW);
         k_anderson_update<<<eg, 256, 0, cs>>>(n2, c->st, b.v1, b.Gv, b.dG, ldF);
         k_finish_once<<<eg, 256, 0, cs>>>(n2, c->st, o->exit_picard_step, b.v1, b.Gv, b.vbest);
         k_mark_finished<<<1, 32, 0, cs>>>(c->st);
-        c->launches += 7;
+        c->launches += 5;
     }
     if ((rc = batch_join(B, B->ev_join2))) return rc;
     CO_CK(cudaGetLastError());

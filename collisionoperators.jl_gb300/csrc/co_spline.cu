@@ -123,61 +123,67 @@ k_locate_hist(co_locate_job j0, co_locate_job j1, int N, const double *__restric
         J.hist[(size_t)blockIdx.x * n_el + i] = hs[i];
 }
 
-// per cell: exclusive offsets of each chunk within the cell, and the count
-__global__ void k_cellcount(co_sortset s0, co_sortset s1, int nchunk, int n_el) {
+// Per cell: exclusive offsets of each chunk within the cell, and the count;
+// then the last block of each marker set to finish (arrival counter
+// tickets[set]) forms the exclusive scan of the counts, cstart[0..n_el] (the
+// cell starts of the sorted order). Integer sums: exact, whatever the order.
+__global__ void __launch_bounds__(256)
+k_cellcount(co_sortset s0, co_sortset s1, int nchunk, int n_el, unsigned *tickets) {
     const co_sortset S = blockIdx.y ? s1 : s0;
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n_el) return;
-    const int *__restrict__ hist = S.hist;
-    int *__restrict__ hoff = S.hoff;
-    int run = 0, k = 0;
-    // eight chunk counts loaded ahead of the running sum: one L2 round trip
-    // per eight chunks instead of per chunk
-    for (; k + 8 <= nchunk; k += 8) {
-        int h[8];
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < n_el) {
+        const int *__restrict__ hist = S.hist;
+        int *__restrict__ hoff = S.hoff;
+        int run = 0, k = 0;
+        // eight chunk counts loaded ahead of the running sum: one L2 round trip
+        // per eight chunks instead of per chunk
+        for (; k + 8 <= nchunk; k += 8) {
+            int h[8];
 #pragma unroll
-        for (int u = 0; u < 8; u++) h[u] = hist[(size_t)(k + u) * n_el + c];
+            for (int u = 0; u < 8; u++) h[u] = hist[(size_t)(k + u) * n_el + c];
 #pragma unroll
-        for (int u = 0; u < 8; u++) {
-            hoff[(size_t)(k + u) * n_el + c] = run;
-            run += h[u];
+            for (int u = 0; u < 8; u++) {
+                hoff[(size_t)(k + u) * n_el + c] = run;
+                run += h[u];
+            }
         }
+        for (; k < nchunk; k++) {
+            int h = hist[(size_t)k * n_el + c];
+            hoff[(size_t)k * n_el + c] = run;
+            run += h;
+        }
+        S.count[c] = run;
     }
-    for (; k < nchunk; k++) {
-        int h = hist[(size_t)k * n_el + c];
-        hoff[(size_t)k * n_el + c] = run;
-        run += h;
-    }
-    S.count[c] = run;
-}
-
-// exclusive scan of count[0..n) -> cstart[0..n]; one block of 1024 threads per set
-__global__ void __launch_bounds__(1024)
-k_cellscan(co_sortset s0, co_sortset s1, int n) {
-    __shared__ int sh[1024];
-    const co_sortset S = blockIdx.y ? s1 : s0;
-    const int *__restrict__ count = S.count;
-    int *__restrict__ cstart = S.cstart;
-    int per = (n + 1023) / 1024;
-    int t = threadIdx.x;
-    int b0 = t * per, b1 = min(n, b0 + per);
-    int s = 0;
-    for (int i = b0; i < b1; i++) s += count[i];
-    sh[t] = s;
+    __shared__ int last;
+    __threadfence();
     __syncthreads();
-    // Hillis-Steele inclusive scan of the 1024 thread sums
-    for (int o = 1; o < 1024; o <<= 1) {
-        int v = t >= o ? sh[t - o] : 0;
+    if (threadIdx.x == 0) last = atomicAdd(&tickets[blockIdx.y], 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (threadIdx.x == 0) tickets[blockIdx.y] = 0u;
+    // exclusive scan of count[0..n_el) by this block; the counts of the other
+    // blocks are read through L2 (__ldcg), past this SM's L1
+    __shared__ int sh[256];
+    const int t = threadIdx.x, nt = blockDim.x;
+    const int per = (n_el + nt - 1) / nt;
+    const int b0 = t * per, b1 = min(n_el, b0 + per);
+    int sum = 0;
+    for (int i = b0; i < b1; i++) sum += __ldcg(&S.count[i]);
+    sh[t] = sum;
+    __syncthreads();
+    for (int o = 1; o < nt; o <<= 1) {   // Hillis-Steele inclusive scan of the thread sums
+        const int v = t >= o ? sh[t - o] : 0;
         __syncthreads();
         sh[t] += v;
         __syncthreads();
     }
     int run = t > 0 ? sh[t - 1] : 0;
     for (int i = b0; i < b1; i++) {
-        cstart[i] = run;
-        run += count[i];
+        S.cstart[i] = run;
+        run += __ldcg(&S.count[i]);
     }
-    if (t == 1023) cstart[n] = sh[1023];
+    if (t == nt - 1) S.cstart[n_el] = sh[nt - 1];
 }
 
 // Stable placement: rank of each marker among the markers of its cell that
@@ -344,6 +350,53 @@ k_mass1(const double *__restrict__ Minv1, const double *__restrict__ b0,
     const double r = co_warp_sum<MASS_OUT>(s, lane);   // output lane >> 2
     const int o = lane >> 2;
     if ((lane & 3) == 0 && i1b + o < nd1) y[(size_t)i2 * nd1 + i1b + o] = r;
+}
+
+// The dof gather and the first mass product in one launch: one block per
+// column i2 (and marker set, blockIdx.y) gathers b[:, i2] from the cell-local
+// entries src[e][9] into shared memory (k_dofgather's sums), then its warps form
+// the outputs of k_mass1 for that column, eight per warp, with k_mass1's
+// arithmetic. Dynamic shared memory: nd1 doubles.
+__global__ void __launch_bounds__(256)
+k_gather_mass1(const double *__restrict__ src0, double *__restrict__ y0,
+               const double *__restrict__ src1, double *__restrict__ y1,
+               const double *__restrict__ Minv1, int n1, int n2, int nd1, int nd2) {
+    extern __shared__ double col[];
+    const double *__restrict__ src = blockIdx.y ? src1 : src0;
+    double *__restrict__ y = blockIdx.y ? y1 : y0;
+    const int i2 = blockIdx.x;
+    for (int k1 = threadIdx.x; k1 < nd1; k1 += blockDim.x) {
+        double acc = 0.0;
+        for (int b = 0; b < 3; b++) {
+            int jj = i2 - b;
+            if (jj < 0 || jj >= n2) continue;
+            for (int a = 0; a < 3; a++) {
+                int i = k1 - a;
+                if (i < 0 || i >= n1) continue;
+                acc += src[(size_t)(i + jj * n1) * 9 + a + 3 * b];
+            }
+        }
+        col[k1] = acc;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int ng1 = (nd1 + MASS_OUT - 1) / MASS_OUT;
+    for (int g = warp; g < ng1; g += nw) {
+        const int i1b = g * MASS_OUT;
+        double s[MASS_OUT];
+#pragma unroll
+        for (int o = 0; o < MASS_OUT; o++) s[o] = 0.0;
+        for (int k = lane; k < nd1; k += 32) {
+            const double bk = col[k];
+            const double *mrow = Minv1 + (size_t)k * nd1;
+#pragma unroll
+            for (int o = 0; o < MASS_OUT; o++)
+                if (i1b + o < nd1) s[o] = fma(mrow[i1b + o], bk, s[o]);
+        }
+        const double r = co_warp_sum<MASS_OUT>(s, lane);   // output lane >> 2
+        const int o = lane >> 2;
+        if ((lane & 3) == 0 && i1b + o < nd1) y[(size_t)i2 * nd1 + i1b + o] = r;
+    }
 }
 
 // out[i1, i2] = sum_k y[i1, k] M2^{-1}[k, i2]
@@ -584,7 +637,7 @@ k_grad_L(const double *__restrict__ x, int N, const int *__restrict__ cell,
          const double *__restrict__ IH1, const double *__restrict__ IH2,
          const double *__restrict__ P1, const double *__restrict__ P2,
          double *__restrict__ G, const double *__restrict__ w, double *__restrict__ dS,
-         const double *__restrict__ dv, double *__restrict__ red) {
+         const double *__restrict__ dv, double *__restrict__ red, co_lambda_job lam) {
     __shared__ double sh[32];
     double pdot = 0.0, pn2 = 0.0;
     for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < N; a += gridDim.x * blockDim.x) {
@@ -632,6 +685,35 @@ k_grad_L(const double *__restrict__ x, int N, const int *__restrict__ cell,
         if (threadIdx.x == 0) {
             red[blockIdx.x * 2 + 0] = s;
             red[blockIdx.x * 2 + 1] = n;
+        }
+        if (lam.st) {
+            // the last block to finish forms the Gonzalez lambda (landau_geff!,
+            // solver.jl:98-103) from all blocks' partials: S1 = S(v_in) from the
+            // element entropy partials (if given), then lambda = (S1 - S0 - dv.dS)
+            // / |dv|^2, the sums in the order of one 256-thread block
+            __shared__ int last;
+            __threadfence();
+            __syncthreads();
+            if (threadIdx.x == 0) last = atomicAdd(lam.ticket, 1u) == gridDim.x - 1;
+            __syncthreads();
+            if (!last) return;
+            __threadfence();
+            if (threadIdx.x == 0) *lam.ticket = 0u;
+            const int nb = gridDim.x;
+            double S1 = lam.Ep ? co_block_sum(co_strided_sum(lam.Ep, threadIdx.x, lam.n_el,
+                                                             blockDim.x, 1, 0, 0.0), sh)
+                               : 0.0;
+            double dot = co_block_sum(co_strided_sum_cg(red, threadIdx.x, nb, blockDim.x, 2, 0,
+                                                        0.0), sh);
+            double nn = co_block_sum(co_strided_sum_cg(red, threadIdx.x, nb, blockDim.x, 2, 1,
+                                                       0.0), sh);
+            if (threadIdx.x == 0) {
+                if (lam.Ep) lam.st->S1 = S1;
+                else S1 = lam.st->S1;
+                double l = 0.0;
+                if (lam.gonzalez) l = nn > 1e-30 ? (S1 - lam.S0 - dot) / nn : 0.0;
+                lam.st->lambda = l;
+            }
         }
     }
 }
@@ -871,9 +953,8 @@ static int sort_sets(co_ctx *c, const co_locate_job &j0, const co_locate_job &j1
         if (nsets > 1) CO_CK(cudaMemsetAsync(s1.hist, 0, sizeof(int) * c->n_el, c->stream));
     }
     k_cellcount<<<dim3(co_cdiv(c->n_el, 256), nsets), 256, 0, c->stream>>>(
-        s0, s1, N > 0 ? nchunk : 1, c->n_el);
-    k_cellscan<<<dim3(1, nsets), 1024, 0, c->stream>>>(s0, s1, c->n_el);
-    c->launches += 2;
+        s0, s1, N > 0 ? nchunk : 1, c->n_el, c->tickets);
+    c->launches++;
     if (N > 0) {
         k_perm<<<dim3(nchunk, nsets), CO_CHUNK, sm, c->stream>>>(s0, s1, N, c->n_el, c->n1,
                                                                  b.w, c->P1, c->P2);
@@ -918,15 +999,26 @@ int co_mass_solve_dev(co_ctx *c, const double *rhs, double *out) {
     return mass_solve_two(c, rhs, c->y, out, rhs, c->y, out, 1);
 }
 
+// cell sums -> (dof gather + M1^{-1}) -> M2^{-1}, for one or two marker sets
+static int gather_solve_two(co_ctx *c, const double *e0, double *y0, double *o0,
+                            const double *e1, double *y1, double *o1, int nsets) {
+    k_gather_mass1<<<dim3(c->nd2, nsets), 256, sizeof(double) * c->nd1, c->stream>>>(
+        e0, y0, e1, y1, c->Minv1, c->n1, c->n2, c->nd1, c->nd2);
+    const int nw = co_cdiv(c->nd1, MASS_OUT) * c->nd2;
+    k_mass2<<<dim3(co_cdiv(nw, 8), nsets), 256, 0, c->stream>>>(c->Minv2, y0, o0, y1, o1,
+                                                                 c->nd1, c->nd2);
+    c->launches += 2;
+    CO_CK(cudaGetLastError());
+    return CO_OK;
+}
+
 int co_project_two(co_ctx *c, double *f0, double *f1, int two) {
     const int nsets = two ? 2 : 1;
     const co_sortset s0 = primary_set(c), s1 = two ? c->gs : s0;
     k_cellsum<<<dim3(c->n_el, nsets), 128, 0, c->stream>>>(s0, s1, c->n_el);
-    k_dofgather<<<dim3(co_cdiv(c->n_dofs, 128), nsets), 128, 0, c->stream>>>(
-        s0.bS, s0.b, s1.bS, s1.b, c->n1, c->n2, c->nd1, c->nd2);
-    c->launches += 2;
+    c->launches++;
     CO_CK(cudaGetLastError());
-    return mass_solve_two(c, s0.b, s0.y, f0, s1.b, s1.y, two ? f1 : f0, nsets);
+    return gather_solve_two(c, s0.bS, s0.y, f0, s1.bS, s1.y, two ? f1 : f0, nsets);
 }
 
 // after co_sort_markers: b = scatter, f = M^{-1} b
@@ -943,6 +1035,17 @@ int co_r_and_entropy_dev(co_ctx *c, const double *f, double *r, const double *fS
     c->launches += 2;
     CO_CK(cudaGetLastError());
     return CO_OK;
+}
+
+int co_r_solve_dev(co_ctx *c, const double *f, double *L, const double *fS) {
+    co_elem_job jr = {f, 0, c->E};
+    co_elem_job js = {fS, 1, c->Ep};
+    k_elem<<<dim3(co_cdiv(c->n_el, ELEM_THREADS / c->nq), fS ? 2 : 1), ELEM_THREADS, 0,
+             c->stream>>>(jr, js, c->n1, c->n2, c->nd1, c->nq, c->Tq1, c->Tq2, c->qw, c->bp1,
+                          c->bp2, (c->flags & CO_FLAG_LOGSQ) ? 1 : 0);
+    c->launches++;
+    CO_CK(cudaGetLastError());
+    return gather_solve_two(c, c->E, c->y, L, c->E, c->y, L, 1);
 }
 
 int co_compute_r_dev(co_ctx *c, const double *f, double *r) {
@@ -995,9 +1098,23 @@ static int red_grid(co_ctx *c, int N) {
 int co_grad_L_dev(co_ctx *c, const double *x, int N, const double *L, double *G,
                   const double *w, double *dS, const double *dv, double *red) {
     if (N == 0) return CO_OK;
+    co_lambda_job none = {};
     k_grad_L<<<red_grid(c, N), CO_RED_THREADS, 0, c->stream>>>(
         x, N, c->mb.cell, c->mb.xi, L, c->n1, c->nd1, c->ih1, c->ih2, c->P1, c->P2, G, w, dS, dv,
-        red);
+        red, none);
+    c->launches++;
+    CO_CK(cudaGetLastError());
+    return CO_OK;
+}
+
+int co_grad_L_lambda_dev(co_ctx *c, const double *x, int N, const double *L, double *G,
+                         const double *w, double *dS, const double *dv, double *red,
+                         double S0, int gonzalez, const double *Ep) {
+    if (N == 0) return CO_ERR_ARG;
+    co_lambda_job lam = {c->st, S0, gonzalez, Ep, c->n_el, c->tickets + CO_TICKET_LAMBDA};
+    k_grad_L<<<red_grid(c, N), CO_RED_THREADS, 0, c->stream>>>(
+        x, N, c->mb.cell, c->mb.xi, L, c->n1, c->nd1, c->ih1, c->ih2, c->P1, c->P2, G, w, dS, dv,
+        red, lam);
     c->launches++;
     CO_CK(cudaGetLastError());
     return CO_OK;
