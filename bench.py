@@ -306,7 +306,7 @@ def run_gpu(args, cfg):
     if args.warmstart == "learned":
         if not os.path.exists(args.warmstart_file):
             raise SystemExit(f"warm-start weights not found: {args.warmstart_file}")
-        warm = learned.WarmStart.load(args.warmstart_file, device=local)
+        warm = learned.WarmStart.load(args.warmstart_file, device=local, relax=args.warm_relax)
     mlp_h = warm.mlp.h if warm is not None else None
     o_head = opts(args.form)
 
@@ -574,7 +574,8 @@ def run_gpu(args, cfg):
                               "metric_freeze": args.dc_metric_freeze,
                               "cap_abort": args.dc_cap_abort,
                               "cap_refresh": args.dc_cap_refresh},
-                   "warmstart": args.warmstart, "retry": bool(args.retry),
+                   "warmstart": args.warmstart, "warm_relax": args.warm_relax,
+                   "retry": bool(args.retry),
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "256 MB buffer written before each timed step"},
         "timed_steps": f"{args.steps} consecutive time steps from the initial markers; a "
@@ -592,9 +593,11 @@ def run_gpu(args, cfg):
             "starts": {s: sum(1 for r in recs if r["start"] == s)
                        for s in ("learned", "predictor", "previous")},
             "retries": sum(1 for r in recs if r["attempts"] > 1),
-            "rule": "start with the smallest first residual among the learned proposal, the "
-                    "explicit predictor and the previous-step state; a solve that does not "
-                    "converge is repeated once from the next start"}
+            "relax": args.warm_relax,
+            "rule": "start with the smallest first residual among the learned proposal "
+                    "(v_pred + relax dt^2 delta), the explicit predictor and the previous-step "
+                    "state; a solve that does not converge is repeated once from the next "
+                    "start"}
             if warm is not None else {"kind": "explicit predictor or previous-step state"}),
         "roofline": dominant, "roofline_fp64": r64, "roofline_fp32": r32, "roofline_ds": rds,
         "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": int(launches),
@@ -755,6 +758,8 @@ def main(argv=None):
     ap.add_argument("--warmstart", choices=["learned", "euler"], default="learned")
     ap.add_argument("--warmstart-file", default=os.path.join(
         PKG, "collops", "warmstart_c3.npz"))
+    ap.add_argument("--warm-relax", type=float, default=0.75,
+                    help="under-relaxation of the learned proposal: v_pred + relax dt^2 delta")
     ap.add_argument("--no-retry", dest="retry", action="store_false",
                     help="do not repeat a non-converged solve from the next start")
     ap.add_argument("--logsq", type=int, choices=[0, 1], default=None,

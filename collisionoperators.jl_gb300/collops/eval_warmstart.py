@@ -64,7 +64,8 @@ def run(weights: str, steps: int = 3, solver: str = "anderson", form: str = "mix
     ws = co.build_workspace(p, device=device)
     lib, h = ws.lib, ws.h
     stream = torch.cuda.ExternalStream(ws.stream(), device=device)
-    warm = learned.WarmStart.load(weights, device=device)
+    # the benchmark's under-relaxed proposal (v_pred + 0.75 dt^2 delta)
+    warm = learned.WarmStart.load(weights, device=device, relax=0.75)
     N, dt = cfg["N"], cfg["dt"]
     v_np, w_np = bimodal_markers(N, cfg["peak"], cfg["T"], cfg["seed"])
     dev = torch.device("cuda", device)

@@ -124,18 +124,22 @@ def features(ws: Workspace, opts: CoOpts, v, w, S0: float, dt: float):
 class WarmStart:
     """Normalisation + network; `propose` implements the learned warm start."""
 
-    def __init__(self, mlp: MLP | None = None, device: int = 0):
+    def __init__(self, mlp: MLP | None = None, device: int = 0, relax: float = 1.0):
         self.mlp = mlp or MLP(device=device)
         self.xm = np.zeros(self.mlp.n_in)
         self.xs = np.ones(self.mlp.n_in)
         self.tm = np.zeros(self.mlp.n_out)
         self.ts = np.ones(self.mlp.n_out)
+        # under-relaxation of the proposal: v = v_pred + relax dt^2 delta
+        self.relax = float(relax)
 
     def _push_normalization(self) -> None:
         """Hand the normalisation to the network: its forward kernel then takes
-        raw features and returns delta itself (co_mlp_set_normalization)."""
+        raw features and returns relax * delta itself (co_mlp_set_normalization;
+        the output mean and scale carry the relaxation factor)."""
         d = lambda a: np.ascontiguousarray(a, dtype=np.float64)  # noqa: E731
-        xm, xs, tm, ts = d(self.xm), d(self.xs), d(self.tm), d(self.ts)
+        xm, xs = d(self.xm), d(self.xs)
+        tm, ts = d(self.tm * self.relax), d(self.ts * self.relax)
         _check(self.mlp.lib.co_mlp_set_normalization(self.mlp.h, _p(xm), _p(xs), _p(tm), _p(ts)),
                "co_mlp_set_normalization")
 
@@ -213,9 +217,11 @@ class WarmStart:
                             tm=self.tm, ts=self.ts)
 
     @classmethod
-    def load(cls, path: str, device: int = 0) -> "WarmStart":
+    def load(cls, path: str, device: int = 0, relax: float = 1.0) -> "WarmStart":
+        """The trained network and its normalisation from `path`; relax < 1
+        under-relaxes the proposal (v_pred + relax dt^2 delta)."""
         z = np.load(path)
-        ws = cls(device=device)
+        ws = cls(device=device, relax=relax)
         if z["params"].size != ws.mlp.P or z["xm"].size != ws.mlp.n_in:
             raise CollopsError(f"{path}: {z['xm'].size}-feature network, this library builds "
                                f"{ws.mlp.n_in} features per marker; retrain with "
