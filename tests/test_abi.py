@@ -145,3 +145,43 @@ def test_checkpoint_roundtrip(collops_mod, tmp_path):
     assert np.array_equal(d["f_coeffs"], f) and d["momentum_history"].shape == (2, 2)
     assert list(d["iter_history"]) == [0, 17]
     assert collops_mod.load_checkpoint("run", 25, directory=str(tmp_path))["step"] == 25
+
+
+def _header_structs():
+    """{typedef name: [(C type, field name, array length or 0)]} of the plain
+    typedef structs in include/collops.h (comments stripped)."""
+    import re
+    src = open(os.path.join(ROOT, "include", "collops.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    src = re.sub(r"//[^\n]*", "", src)
+    out = {}
+    for body, name in re.findall(r"typedef struct\s*\{(.*?)\}\s*(\w+)\s*;", src, flags=re.S):
+        fields = []
+        for decl in body.split(";"):
+            decl = " ".join(decl.split())
+            if not decl:
+                continue
+            m = re.match(r"(.*?)(\w+)\s*(?:\[(\d+)\])?$", decl)
+            ctype, fname, n = m.group(1).strip(), m.group(2), int(m.group(3) or 0)
+            fields.append((ctype, fname, n))
+        out[name] = fields
+    return out
+
+
+@pytest.mark.parametrize("cname,pyname", [("co_opts", "CoOpts"),
+                                          ("co_defect_opts", "CoDefectOpts"),
+                                          ("co_newton_opts", "CoNewtonOpts"),
+                                          ("co_step_info", "CoStepInfo")])
+def test_ctypes_mirrors_match_header(collops_mod, cname, pyname):
+    """The Python mirrors of the option and record structs have the header's
+    fields, in its order, with its types (a field added on one side only would
+    shift every later field across the C ABI)."""
+    ctypes_of = {"int": C.c_int, "double": C.c_double, "unsigned": C.c_uint,
+                 "unsigned long long": C.c_ulonglong}
+    hdr = _header_structs()[cname]
+    py = getattr(collops_mod, pyname)._fields_
+    assert [f for _, f, _ in hdr] == [f for f, _ in py]
+    for (ctype, fname, n), (_, pytype) in zip(hdr, py):
+        want = ctypes_of[ctype] * n if n else ctypes_of[ctype]
+        assert C.sizeof(pytype) == C.sizeof(want) and (
+            pytype == want or getattr(pytype, "_type_", None) == getattr(want, "_type_", None)), fname
